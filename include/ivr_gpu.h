@@ -1,0 +1,191 @@
+/*
+ * ivr_gpu.h -- C ABI of the GB300 (sm_103a) iVR ray-casting hot path.
+ *
+ * Drop-in for the reference's per-frame path.  The reference keeps all state
+ * in process globals (main.c:63-105) and selects variants through function
+ * pointers (ray.h:25, transferfuncs.h:22, colormap.h:22); here the same steps
+ * are explicit calls on opaque handles:
+ *
+ *   reference                                   this ABI
+ *   -----------------------------------------   ------------------------------
+ *   readvoldata / readfromfile (main.c:629,     ivr_volume_load, ivr_volume_load_file
+ *     main.c:1220), byteswap (main.c:695-703)
+ *   initvolattrs / initvolbbox / getlocalbrick  ivr_bricks_setup
+ *     (main.c:387, main.c:505, utils.c:332)
+ *   setviewport / setplaneconst / setmvm /      ivr_set_view (takes the 184-byte
+ *     setpm / setfrustum / updatevolbbox          STATE of connection.h:9-18)
+ *     (mathutil.h:147-233, ray.c:44,
+ *      mathutil.c:948)
+ *   initcolormap / initvolluts /                ivr_tf_set_colormap, ivr_tf_set_lut
+ *     inittransferfunc (colormap.c:183,
+ *     main.c:1075, transferfuncs.c:201)
+ *   createlocalimage (main.c:937)               ivr_render_brick (one brick), and
+ *     + compositelocalimage (main.c:708)        ivr_render / ivr_render_tile (all
+ *     + compositetiles (main.c:1203)              bricks, composited on device)
+ *   compositetiles (main.c:1203)                ivr_composite
+ *   writetomemory RGBA8 rule (main.c:1404)      ivr_quantize (and fused in ivr_render)
+ *
+ * Conventions.  Every call returns an int status: IVR_OK (0) or a negative
+ * IVR_ERR_*; nothing calls exit() or assert().  ivr_last_error() gives the
+ * message of the last failure on a context.  Buffers named *_dev are device
+ * pointers; device work is queued on the caller's stream (a cudaStream_t
+ * passed as void*, NULL = the legacy default stream).  Handles are not
+ * thread-safe: use one context per host thread, or serialise calls.
+ * Images are [h][w] rows of RGBA, row 0 at the bottom (GL raster order).
+ */
+#ifndef IVR_GPU_H
+#define IVR_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IVR_OK 0
+#define IVR_ERR_INVALID (-1)     /* bad argument or handle */
+#define IVR_ERR_CUDA (-2)        /* a CUDA call failed */
+#define IVR_ERR_NOMEM (-3)       /* allocation refused by the HBM budget or by CUDA */
+#define IVR_ERR_IO (-4)          /* volume file missing or short */
+#define IVR_ERR_UNSUPPORTED (-5) /* valid request this build does not serve */
+#define IVR_ERR_TIMEOUT (-6)     /* a bounded device wait gave up */
+
+typedef struct ivr_ctx ivr_ctx;
+typedef struct ivr_volume ivr_volume;
+typedef struct ivr_tf ivr_tf;
+typedef struct ivr_view ivr_view;
+
+/* STATE (connection.h:9-18): the steering message, GL column-major
+ * matrices, 184 bytes. */
+typedef struct ivr_state {
+    int finish, winwidth, winheight;
+    float alpha;        /* opacity scale (mystate.alpha) */
+    float newconst[6];  /* clip plane constants; min()'d with the box (ray.c:44) */
+    float vv[4];        /* view-plane extents l, r, b, t (getfrustum) */
+    float mvm[16];
+    float pm[16];
+} ivr_state;
+
+typedef enum { IVR_U8 = 0, IVR_U16 = 1, IVR_F32 = 2 } ivr_dtype;
+
+/* Transfer functions: ids 0-5 are the reference's (transferfuncs.h:8-13);
+ * IVR_TF_F2B is front-to-back premultiplied compositing with early
+ * termination (the CONFIG preset). */
+typedef enum {
+    IVR_TF_SEISMIC = 0, IVR_TF_MED = 1, IVR_TF_SEISMIC2 = 2, IVR_TF_CHEM = 3,
+    IVR_TF_BLEND = 4, IVR_TF_RGBBLEND = 5, IVR_TF_F2B = 6
+} ivr_tf_mode;
+
+/* Colormap ids (colormap.h:15-20). */
+typedef enum { IVR_CM_BASE = 0, IVR_CM_RAINBOW = 1, IVR_CM_MEDICAL = 2, IVR_CM_SEISMIC = 3,
+               IVR_CM_JET = 4, IVR_CM_NOMAP = -1 } ivr_colormap;
+
+typedef enum { IVR_PRESET_REF = 0, IVR_PRESET_CONFIG = 1 } ivr_preset;
+typedef enum { IVR_ORDER_CENTER = 0, IVR_ORDER_AXIS = 1 } ivr_order;
+typedef enum { IVR_SKIP_NONE = 0, IVR_SKIP_GRID = 1 } ivr_skip;
+
+/* How a frame is sampled.
+ * REF: the reference's sampling exactly (ray.c): ray-parameter step 0.001,
+ *   256-sample cap, its trilinear formula, per-brick lattices, centre-depth
+ *   brick order (sortboxlist), transfer function ids 0-5.
+ * CONFIG: true trilinear, one sample lattice per ray with `step` in voxels,
+ *   no cap, front-to-back compositing stopping at A >= term_alpha, exact
+ *   per-axis brick order. */
+typedef struct ivr_render_params {
+    int preset;        /* ivr_preset */
+    float step;        /* REF: ray-parameter step; CONFIG: voxels */
+    int max_samples;   /* per ray and brick; 0 = unbounded */
+    float term_alpha;  /* early termination threshold (> 1 disables) */
+    int order;         /* ivr_order */
+    int skip;          /* ivr_skip: empty-space skipping (never changes the image) */
+    int tilew, tileh;  /* viewport rounded down to multiples (argv[11..12]) */
+} ivr_render_params;
+
+/* Per-frame geometry ivr_set_view computed, for callers that composite or
+ * tile themselves (the fields of compositelocalimage's bookkeeping). */
+#define IVR_MAX_BRICKS 64
+typedef struct ivr_frame_info {
+    int vw, vh;                        /* viewport after tile rounding */
+    int nbricks;
+    int order[IVR_MAX_BRICKS];         /* composite order, near -> far */
+    float wincoord[IVR_MAX_BRICKS][6]; /* x, y, z, w, h, d (updatevolbbox) */
+    int rect[IVR_MAX_BRICKS][4];       /* istrt, istop, jstrt, jstop */
+} ivr_frame_info;
+
+/* --- context ----------------------------------------------------------- */
+void ivr_params_ref(ivr_render_params *p);     /* REF defaults */
+void ivr_params_config(ivr_render_params *p);  /* CONFIG defaults */
+int ivr_create(int device, size_t hbm_budget_bytes, ivr_ctx **out); /* budget 0 = no limit */
+int ivr_destroy(ivr_ctx *ctx);
+const char *ivr_last_error(const ivr_ctx *ctx);
+int ivr_mem_used(const ivr_ctx *ctx, size_t *bytes);
+/* Samples the march kernels executed since the last reset (a diagnostic
+ * counter: skipped and terminated samples are not counted). */
+int ivr_counters(ivr_ctx *ctx, unsigned long long *samples_exec, int reset);
+
+/* --- volume load / brick setup (readvoldata, readfromfile, initvolbbox) -- */
+/* Copies a host volume (x fastest, [d][h][w]) to the device.  byteswap != 0
+ * reverses the bytes of every element (main.c:695-703 for f32). */
+int ivr_volume_load(ivr_ctx *ctx, const void *host, int w, int h, int d, int dtype,
+                    int byteswap, ivr_volume **out);
+/* Reads a raw volume file.  file_little_endian follows argv[5] of the
+ * reference: the data are byte-swapped when it differs from the host. */
+int ivr_volume_load_file(ivr_ctx *ctx, const char *path, int w, int h, int d, int dtype,
+                         int file_little_endian, ivr_volume **out);
+int ivr_volume_free(ivr_volume *vol);
+/* Splits the volume into py x px x pz bricks (rows, columns, slabs as
+ * argv[8..10]) with `overlap` halo voxels on the high side of inner bricks
+ * (getlocalbrick).  Each brick becomes its own device array.  The default
+ * after load is one brick. */
+int ivr_bricks_setup(ivr_volume *vol, int py, int px, int pz, int overlap);
+/* min, max and the histogram of mathutil.c:444-470 (hist may be NULL;
+ * otherwise it holds hsize = (int)(max-min+1) bins). */
+int ivr_volume_minmax(ivr_volume *vol, float *mn, float *mx);
+int ivr_volume_histogram(ivr_volume *vol, int *hist, int hsize);
+
+/* --- transfer function (initcolormap, initvolluts, inittransferfunc) ---- */
+int ivr_tf_create(ivr_ctx *ctx, ivr_tf **out);
+int ivr_tf_free(ivr_tf *tf);
+/* Direct LUT injection: n RGBA rows; index = (int)(sample*scale) - offset
+ * (scale must be 1 outside IVR_TF_F2B). */
+int ivr_tf_set_lut(ivr_tf *tf, const float *rgba, int n, int lut_offset, float lut_scale, int mode);
+/* The reference's LUT path: histogram + colormap builder over the volume's
+ * global range, lutoffset = (int)(min + 0.5), maxlutindx = hsize - 1. */
+int ivr_tf_set_colormap(ivr_tf *tf, ivr_volume *vol, int colormap, int mode);
+int ivr_tf_get_lut(const ivr_tf *tf, float *rgba, int n, int *lut_n, int *lut_offset);
+
+/* --- view (setviewport ... updatevolbbox) ------------------------------ */
+int ivr_view_create(ivr_ctx *ctx, ivr_view **out);
+int ivr_view_free(ivr_view *view);
+int ivr_set_view(ivr_view *view, ivr_volume *vol, const ivr_state *state, const ivr_render_params *p);
+int ivr_view_info(const ivr_view *view, ivr_frame_info *info);
+
+/* --- render (createlocalimage + compositelocalimage + writetomemory) ---- */
+/* Full viewport, all bricks composited.  rgba32_dev: [vh][vw] float4
+ * (nullable); rgba8_dev: [vh][vw] uchar4 (nullable). */
+int ivr_render(ivr_view *view, ivr_tf *tf, float *rgba32_dev, uint8_t *rgba8_dev, void *stream);
+/* One screen tile [x,x+w) x [y,y+h) of the viewport into [h][w] buffers. */
+int ivr_render_tile(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h,
+                    float *rgba32_dev, uint8_t *rgba8_dev, void *stream);
+/* One brick's sub-image over the whole viewport, zero outside its rect
+ * (createlocalimage(rank)). */
+int ivr_render_brick(ivr_view *view, ivr_tf *tf, int brick, float *rgba32_dev, void *stream);
+/* End to end: STATE from host memory in, RGBA8 frame to host memory out
+ * (pinned staging inside; waits for the frame). */
+int ivr_render_host(ivr_view *view, ivr_volume *vol, ivr_tf *tf, const ivr_state *state,
+                    const ivr_render_params *p, uint8_t *rgba8_host, void *stream);
+
+/* --- compositing and output -------------------------------------------- */
+/* compositetiles (main.c:1203-1218): num sub-images of w*h RGBA floats in
+ * near -> far order, composited far -> near onto tilebuf with
+ * d = s + (1 - s.a) * d. */
+int ivr_composite(ivr_ctx *ctx, float *tilebuf_dev, const float *rcolorbuf_dev, int num,
+                  int w, int h, void *stream);
+/* (uint8)(clamp(v,0,1) * 255 + 0.5) per float (main.c:1404). */
+int ivr_quantize(ivr_ctx *ctx, const float *in_dev, uint8_t *out_dev, long long n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,217 @@
+"""Python handles over the C ABI of libivr_gpu.so.
+
+Device buffers are passed as integer device addresses (for example a torch
+tensor's ``data_ptr()``), streams as integer ``cudaStream_t`` handles (for
+example ``torch.cuda.current_stream().cuda_stream``); ``None`` means null.
+Every call raises ``IvrError`` with the library's message on failure.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import FrameInfo, IvrError, RenderParams
+from .state import IvrState
+
+U8, U16, F32 = 0, 1, 2
+DTYPES = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
+TF_SEISMIC, TF_MED, TF_SEISMIC2, TF_CHEM, TF_BLEND, TF_RGBBLEND, TF_F2B = range(7)
+CM_BASE, CM_RAINBOW, CM_MEDICAL, CM_SEISMIC, CM_JET, CM_NOMAP = 0, 1, 2, 3, 4, -1
+PRESET_REF, PRESET_CONFIG = 0, 1
+ORDER_CENTER, ORDER_AXIS = 0, 1
+SKIP_NONE, SKIP_GRID = 0, 1
+
+
+def _vp(x) -> Optional[int]:
+    return None if x is None else int(x)
+
+
+def ref_params(tile=(1, 1)) -> RenderParams:
+    """The reference's sampling (ray.c): step 0.001, 256-sample cap."""
+    p = RenderParams()
+    _lib.load().ivr_params_ref(ctypes.byref(p))
+    p.tilew, p.tileh = tile
+    return p
+
+
+def config_params(step=0.5, term_alpha=0.99, skip=True, tile=(1, 1)) -> RenderParams:
+    """Benchmark sampling: true trilinear, ``step`` voxels, early termination."""
+    p = RenderParams()
+    _lib.load().ivr_params_config(ctypes.byref(p))
+    p.step = step
+    p.term_alpha = term_alpha
+    p.skip = SKIP_GRID if skip else SKIP_NONE
+    p.tilew, p.tileh = tile
+    return p
+
+
+class Context:
+    """ivr_create / ivr_destroy: one GPU, an optional HBM budget in bytes."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self.lib.ivr_create(device, hbm_budget, ctypes.byref(h))
+        if rc != 0:
+            raise IvrError(rc, f"ivr_create(device={device}) failed")
+        self.h = h
+
+    def check(self, rc: int):
+        if rc != 0:
+            raise IvrError(rc, self.lib.ivr_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.ivr_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def mem_used(self) -> int:
+        v = ctypes.c_size_t()
+        self.check(self.lib.ivr_mem_used(self.h, ctypes.byref(v)))
+        return v.value
+
+    def samples_executed(self, reset: bool = False) -> int:
+        v = ctypes.c_ulonglong()
+        self.check(self.lib.ivr_counters(self.h, ctypes.byref(v), int(reset)))
+        return v.value
+
+    def load_volume(self, vol: np.ndarray, byteswap: bool = False) -> "Volume":
+        """readvoldata: a (d, h, w) uint8/uint16/float32 array to the device."""
+        vol = np.ascontiguousarray(vol)
+        if vol.ndim != 3 or vol.dtype not in DTYPES:
+            raise ValueError("volume must be a 3-D uint8, uint16 or float32 array (d, h, w)")
+        d, h, w = vol.shape
+        out = ctypes.c_void_p()
+        self.check(self.lib.ivr_volume_load(self.h, vol.ctypes.data, w, h, d, DTYPES[vol.dtype], int(byteswap),
+                                            ctypes.byref(out)))
+        return Volume(self, out, (d, h, w), DTYPES[vol.dtype])
+
+    def load_volume_file(self, path: str, w: int, h: int, d: int, dtype: int,
+                         file_little_endian: bool = True) -> "Volume":
+        out = ctypes.c_void_p()
+        self.check(self.lib.ivr_volume_load_file(self.h, path.encode(), w, h, d, dtype, int(file_little_endian),
+                                                 ctypes.byref(out)))
+        return Volume(self, out, (d, h, w), dtype)
+
+    def transfer_function(self) -> "TransferFunction":
+        out = ctypes.c_void_p()
+        self.check(self.lib.ivr_tf_create(self.h, ctypes.byref(out)))
+        return TransferFunction(self, out)
+
+    def view(self) -> "View":
+        out = ctypes.c_void_p()
+        self.check(self.lib.ivr_view_create(self.h, ctypes.byref(out)))
+        return View(self, out)
+
+    def composite(self, tilebuf, rcolorbuf, num: int, w: int, h: int, stream=None):
+        """compositetiles: num w*h RGBA sub-images (near -> far) over tilebuf."""
+        self.check(self.lib.ivr_composite(self.h, _vp(tilebuf), _vp(rcolorbuf), num, w, h, _vp(stream)))
+
+    def quantize(self, src, dst, n: int, stream=None):
+        self.check(self.lib.ivr_quantize(self.h, _vp(src), _vp(dst), n, _vp(stream)))
+
+
+class Volume:
+    def __init__(self, ctx: Context, h, shape, dtype):
+        self.ctx, self.h, self.shape, self.dtype = ctx, h, shape, dtype
+
+    def bricks(self, py: int, px: int, pz: int, overlap: int = 1) -> "Volume":
+        """initvolbbox/getlocalbrick: py rows x px columns x pz slabs."""
+        self.ctx.check(self.ctx.lib.ivr_bricks_setup(self.h, py, px, pz, overlap))
+        return self
+
+    def minmax(self):
+        mn, mx = ctypes.c_float(), ctypes.c_float()
+        self.ctx.check(self.ctx.lib.ivr_volume_minmax(self.h, ctypes.byref(mn), ctypes.byref(mx)))
+        return mn.value, mx.value
+
+    def histogram(self, hsize: int) -> np.ndarray:
+        hist = np.zeros(hsize, dtype=np.int32)
+        self.ctx.check(self.ctx.lib.ivr_volume_histogram(
+            self.h, hist.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), hsize))
+        return hist
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.ivr_volume_free(self.h)
+            self.h = None
+
+
+class TransferFunction:
+    def __init__(self, ctx: Context, h):
+        self.ctx, self.h = ctx, h
+
+    def set_lut(self, rgba: np.ndarray, offset: int = 0, scale: float = 1.0, mode: int = TF_F2B):
+        lut = np.ascontiguousarray(rgba, dtype=np.float32).reshape(-1, 4)
+        self.ctx.check(self.ctx.lib.ivr_tf_set_lut(self.h, lut.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                   len(lut), offset, scale, mode))
+        return self
+
+    def set_colormap(self, vol: Volume, colormap: int, mode: int):
+        """initcolormap + initvolluts + inittransferfunc."""
+        self.ctx.check(self.ctx.lib.ivr_tf_set_colormap(self.h, vol.h, colormap, mode))
+        return self
+
+    def get_lut(self):
+        n, off = ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(self.ctx.lib.ivr_tf_get_lut(self.h, None, 0, ctypes.byref(n), ctypes.byref(off)))
+        out = np.zeros((n.value, 4), dtype=np.float32)
+        self.ctx.check(self.ctx.lib.ivr_tf_get_lut(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                   n.value, None, None))
+        return out, off.value
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.ivr_tf_free(self.h)
+            self.h = None
+
+
+class View:
+    def __init__(self, ctx: Context, h):
+        self.ctx, self.h = ctx, h
+
+    def set(self, vol: Volume, state: IvrState, params: RenderParams) -> "View":
+        """setviewport/setplaneconst/setmvm/setpm/setfrustum/updatevolbbox."""
+        self.ctx.check(self.ctx.lib.ivr_set_view(self.h, vol.h, ctypes.byref(state), ctypes.byref(params)))
+        return self
+
+    def info(self) -> dict:
+        fi = FrameInfo()
+        self.ctx.check(self.ctx.lib.ivr_view_info(self.h, ctypes.byref(fi)))
+        n = fi.nbricks
+        return {"vw": fi.vw, "vh": fi.vh, "nbricks": n, "order": list(fi.order[:n]),
+                "wincoord": [list(fi.wincoord[k]) for k in range(n)], "rect": [list(fi.rect[k]) for k in range(n)]}
+
+    def render(self, tf: TransferFunction, rgba32=None, rgba8=None, stream=None):
+        self.ctx.check(self.ctx.lib.ivr_render(self.h, tf.h, _vp(rgba32), _vp(rgba8), _vp(stream)))
+
+    def render_tile(self, tf: TransferFunction, x, y, w, h, rgba32=None, rgba8=None, stream=None):
+        self.ctx.check(self.ctx.lib.ivr_render_tile(self.h, tf.h, x, y, w, h, _vp(rgba32), _vp(rgba8), _vp(stream)))
+
+    def render_brick(self, tf: TransferFunction, brick: int, rgba32, stream=None):
+        """createlocalimage(rank): one brick's sub-image over the viewport."""
+        self.ctx.check(self.ctx.lib.ivr_render_brick(self.h, tf.h, brick, _vp(rgba32), _vp(stream)))
+
+    def render_host(self, vol: Volume, tf: TransferFunction, state: IvrState, params: RenderParams,
+                    out: np.ndarray, stream=None):
+        """End to end: STATE in, RGBA8 frame to host memory (out: uint8 [vh, vw, 4])."""
+        if out.dtype != np.uint8 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous uint8 array")
+        self.ctx.check(self.ctx.lib.ivr_render_host(self.h, vol.h, tf.h, ctypes.byref(state), ctypes.byref(params),
+                                                    out.ctypes.data, _vp(stream)))
+        return out
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.ivr_view_free(self.h)
+            self.h = None

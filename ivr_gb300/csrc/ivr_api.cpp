@@ -1,0 +1,603 @@
+// ivr_api.cpp -- the C ABI (include/ivr_gpu.h): handles, device memory
+// under an HBM budget, volume load and brick set-up, transfer functions,
+// views and render calls.
+#include <float.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "ivr_frame.h"
+
+struct ivr_ctx {
+    int device = 0;
+    size_t budget = 0;   // 0 = unlimited
+    size_t used = 0;
+    std::string err;
+    unsigned long long *d_counters = nullptr;
+    float *d_partial = nullptr;  // min/max partials
+    uchar4 *d_frame8 = nullptr;  // ivr_render_host staging
+    size_t frame8_bytes = 0;
+    unsigned tf_serial = 0;
+};
+
+struct ivr_volume {
+    ivr_ctx *ctx = nullptr;
+    int w = 0, h = 0, d = 0, dtype = 0;
+    void *d_full = nullptr;
+    size_t full_bytes = 0;
+    std::vector<ivr::HostBrick> bricks;
+    int py = 1, px = 1, pz = 1, overlap = 0;
+    bool have_minmax = false;
+    float vmin = 0.0f, vmax = 0.0f;
+    unsigned empty_serial = 0;  // TF serial the empty flags were built for
+    int empty_zero_alpha = -1;  // whether they were built for alpha == 0
+};
+
+struct ivr_tf {
+    ivr_ctx *ctx = nullptr;
+    int n = 0, off = 0, mode = IVR_TF_SEISMIC;
+    float scale = 1.0f;
+    float4 *d_lut = nullptr;
+    int *d_nzprefix = nullptr;
+    int cap = 0;
+    std::vector<float> host;
+    unsigned serial = 0;
+};
+
+struct ivr_view {
+    ivr_ctx *ctx = nullptr;
+    ivr_volume *vol = nullptr;
+    ivr_render_params p{};
+    ivr_state st{};
+    bool valid = false;
+    ivr::FrameDesc f{};
+    ivr_frame_info info{};
+};
+
+namespace {
+
+using namespace ivr;
+
+int fail(ivr_ctx *c, int code, const char *fmt, ...)
+{
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+int cuda_fail(ivr_ctx *c, cudaError_t e, const char *what)
+{
+    return fail(c, IVR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(ctx, call)                                                   \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call);      \
+    } while (0)
+
+int dev_alloc(ivr_ctx *c, size_t bytes, void **p)
+{
+    *p = nullptr;
+    if (bytes == 0) return IVR_OK;
+    if (c->budget && c->used + bytes > c->budget)
+        return fail(c, IVR_ERR_NOMEM, "HBM budget: %zu + %zu bytes exceeds %zu", c->used, bytes, c->budget);
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(c, IVR_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    c->used += bytes;
+    return IVR_OK;
+}
+
+void dev_free(ivr_ctx *c, void *p, size_t bytes)
+{
+    if (!p) return;
+    cudaFree(p);
+    c->used -= bytes;
+}
+
+size_t brick_bytes(const ivr_volume *v, const HostBrick &b)
+{
+    return (size_t) b.lw * b.lh * b.ld * dtype_size(v->dtype);
+}
+
+size_t mc_cells(const HostBrick &b) { return (size_t) b.mcx * b.mcy * b.mcz; }
+
+void free_bricks(ivr_volume *v)
+{
+    for (auto &b : v->bricks) {
+        if (b.owns) dev_free(v->ctx, b.data, brick_bytes(v, b));
+        dev_free(v->ctx, b.mc_minmax, mc_cells(b) * 2 * sizeof(float));
+        dev_free(v->ctx, b.empty, mc_cells(b));
+    }
+    v->bricks.clear();
+    v->empty_serial = 0;
+    v->empty_zero_alpha = -1;
+}
+
+// macrocell grid over a brick's local voxels (cells of kCell, +1 layer)
+int build_macrocells(ivr_volume *v, HostBrick &b)
+{
+    b.mcx = (b.lw - 2) / kCell + 1;
+    b.mcy = (b.lh - 2) / kCell + 1;
+    b.mcz = (b.ld - 2) / kCell + 1;
+    int rc = dev_alloc(v->ctx, mc_cells(b) * 2 * sizeof(float), (void **) &b.mc_minmax);
+    if (rc) return rc;
+    rc = dev_alloc(v->ctx, mc_cells(b), (void **) &b.empty);
+    if (rc) return rc;
+    CK(v->ctx, launch_macrocells(b.data, v->dtype, b.lw, b.lh, b.ld, b.mc_minmax, b.mcx, b.mcy, b.mcz, 0));
+    return IVR_OK;
+}
+
+int setup_bricks(ivr_volume *v, int py, int px, int pz, int overlap)
+{
+    ivr_ctx *c = v->ctx;
+    if (py < 1 || px < 1 || pz < 1 || py * px * pz > kMaxBricks || overlap < 0 || overlap > 1)
+        return fail(c, IVR_ERR_INVALID, "brick grid %dx%dx%d (overlap %d) not supported", py, px, pz, overlap);
+    if (v->w / px < 2 || v->h / py < 2 || v->d / pz < 2)
+        return fail(c, IVR_ERR_INVALID, "bricks of %dx%dx%d voxels are too thin", v->w / px, v->h / py, v->d / pz);
+    free_bricks(v);
+    int K = py * px * pz;
+    v->bricks.resize(K);
+    for (int r = 0; r < K; r++) {
+        HostBrick &b = v->bricks[r];
+        memset(&b, 0, sizeof(b));
+        brick_geometry(v->w, v->h, v->d, py, px, pz, overlap, r, b);
+        if (K == 1) {
+            b.data = v->d_full;
+            b.owns = false;
+        } else {
+            int rc = dev_alloc(c, brick_bytes(v, b), &b.data);
+            if (rc) { free_bricks(v); return rc; }
+            b.owns = true;
+            CK(c, launch_gather_brick(v->d_full, v->w, v->h, v->d, b.data, b.sx, b.sy, b.sz, b.lw, b.lh, b.ld,
+                                      (int) dtype_size(v->dtype), 0));
+        }
+        int rc = build_macrocells(v, b);
+        if (rc) { free_bricks(v); return rc; }
+    }
+    CK(c, cudaDeviceSynchronize());
+    v->py = py; v->px = px; v->pz = pz; v->overlap = overlap;
+    return IVR_OK;
+}
+
+int valid_params(ivr_ctx *c, const ivr_render_params *p)
+{
+    if (!p) return fail(c, IVR_ERR_INVALID, "null render params");
+    if (p->preset != IVR_PRESET_REF && p->preset != IVR_PRESET_CONFIG)
+        return fail(c, IVR_ERR_INVALID, "unknown preset %d", p->preset);
+    if (!(p->step > 0.0f)) return fail(c, IVR_ERR_INVALID, "step must be > 0");
+    if (p->tilew < 1 || p->tileh < 1) return fail(c, IVR_ERR_INVALID, "tile size must be >= 1");
+    return IVR_OK;
+}
+
+// Per-brick empty-cell flags for a TF (cached by TF serial and by whether
+// the opacity scale is zero).
+int refresh_empty(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s)
+{
+    if (v->empty_serial == tf->serial && v->empty_zero_alpha == (int) zero_alpha) return IVR_OK;
+    for (auto &b : v->bricks) {
+        if (zero_alpha) CK(v->ctx, cudaMemsetAsync(b.empty, 1, mc_cells(b), s));
+        else CK(v->ctx, launch_empty_flags(b.mc_minmax, (int) mc_cells(b), tf->d_nzprefix, tf->n, tf->off,
+                                           tf->scale, b.empty, s));
+    }
+    v->empty_serial = tf->serial;
+    v->empty_zero_alpha = (int) zero_alpha;
+    return IVR_OK;
+}
+
+int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single, float *o32, uint8_t *o8,
+                  void *stream)
+{
+    ivr_ctx *c = view ? view->ctx : nullptr;
+    if (!view || !tf) return fail(c, IVR_ERR_INVALID, "null view or transfer function");
+    if (!view->valid) return fail(c, IVR_ERR_INVALID, "ivr_set_view has not succeeded on this view");
+    if (tf->mode != IVR_TF_RGBBLEND && tf->n < 1) return fail(c, IVR_ERR_INVALID, "transfer function has no LUT");
+    const bool f2b = tf->mode == IVR_TF_F2B;
+    if ((view->p.preset == IVR_PRESET_CONFIG) != f2b)
+        return fail(c, IVR_ERR_UNSUPPORTED, "CONFIG preset needs IVR_TF_F2B and REF needs ids 0-5 (got %d)", tf->mode);
+    if (x < 0 || y < 0 || w < 1 || h < 1 || x + w > view->info.vw || y + h > view->info.vh)
+        return fail(c, IVR_ERR_INVALID, "tile %d,%d %dx%d outside the %dx%d viewport", x, y, w, h, view->info.vw,
+                    view->info.vh);
+    cudaStream_t s = (cudaStream_t) stream;
+    FrameDesc f = view->f;
+    f.tf_mode = tf->mode;
+    f.lut = tf->d_lut;
+    f.lut_n = tf->n;
+    f.lut_off = tf->off;
+    f.lut_scale = tf->scale;
+    f.out_x = x; f.out_y = y; f.out_w = w; f.out_h = h;
+    f.single = single;
+    f.counters = c->d_counters;
+    const bool skip = view->p.skip == IVR_SKIP_GRID && view->p.preset == IVR_PRESET_CONFIG;
+    if (skip) {
+        int rc = refresh_empty(view->vol, tf, !(f.alpha != 0.0f), s);
+        if (rc) return rc;
+        for (int k = 0; k < f.nb; k++) f.b[k].empty = view->vol->bricks[k].empty;
+    }
+    CK(c, launch_march(f, (float4 *) o32, (uchar4 *) o8, s));
+    return IVR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void ivr_params_ref(ivr_render_params *p)
+{
+    if (!p) return;
+    p->preset = IVR_PRESET_REF;
+    p->step = 0.001f;  // DELTASAMPLE (types.h:17)
+    p->max_samples = 256;  // MAXVOLUMESAMPLES * 4 (ray.c:61)
+    p->term_alpha = 2.0f;
+    p->order = IVR_ORDER_CENTER;
+    p->skip = IVR_SKIP_NONE;
+    p->tilew = 1;
+    p->tileh = 1;
+}
+
+void ivr_params_config(ivr_render_params *p)
+{
+    if (!p) return;
+    p->preset = IVR_PRESET_CONFIG;
+    p->step = 0.5f;
+    p->max_samples = 0;
+    p->term_alpha = 0.99f;
+    p->order = IVR_ORDER_AXIS;
+    p->skip = IVR_SKIP_GRID;
+    p->tilew = 1;
+    p->tileh = 1;
+}
+
+int ivr_create(int device, size_t budget, ivr_ctx **out)
+{
+    if (!out) return IVR_ERR_INVALID;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return IVR_ERR_CUDA;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return IVR_ERR_CUDA;
+    ivr_ctx *c = new ivr_ctx();
+    c->device = device;
+    c->budget = budget;
+    if (dev_alloc(c, sizeof(unsigned long long) * 4, (void **) &c->d_counters) ||
+        dev_alloc(c, sizeof(float) * 2 * minmax_parts(), (void **) &c->d_partial)) {
+        ivr_destroy(c);
+        return IVR_ERR_NOMEM;
+    }
+    cudaMemset(c->d_counters, 0, sizeof(unsigned long long) * 4);
+    *out = c;
+    return IVR_OK;
+}
+
+int ivr_destroy(ivr_ctx *c)
+{
+    if (!c) return IVR_ERR_INVALID;
+    cudaSetDevice(c->device);
+    dev_free(c, c->d_counters, sizeof(unsigned long long) * 4);
+    dev_free(c, c->d_partial, sizeof(float) * 2 * minmax_parts());
+    dev_free(c, c->d_frame8, c->frame8_bytes);
+    delete c;
+    return IVR_OK;
+}
+
+const char *ivr_last_error(const ivr_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int ivr_mem_used(const ivr_ctx *c, size_t *bytes)
+{
+    if (!c || !bytes) return IVR_ERR_INVALID;
+    *bytes = c->used;
+    return IVR_OK;
+}
+
+int ivr_counters(ivr_ctx *c, unsigned long long *samples_exec, int reset)
+{
+    if (!c) return IVR_ERR_INVALID;
+    if (samples_exec) CK(c, cudaMemcpy(samples_exec, c->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    if (reset) CK(c, cudaMemset(c->d_counters, 0, sizeof(unsigned long long) * 4));
+    return IVR_OK;
+}
+
+int ivr_volume_load(ivr_ctx *c, const void *host, int w, int h, int d, int dtype, int byteswap, ivr_volume **out)
+{
+    if (!c || !out) return IVR_ERR_INVALID;
+    *out = nullptr;
+    if (!host) return fail(c, IVR_ERR_INVALID, "null volume data");
+    if (w < 2 || h < 2 || d < 2) return fail(c, IVR_ERR_INVALID, "volume %dx%dx%d: every dimension must be >= 2", w, h, d);
+    if (dtype != IVR_U8 && dtype != IVR_U16 && dtype != IVR_F32) return fail(c, IVR_ERR_INVALID, "dtype %d", dtype);
+    if ((long long) w * h * d >= (1LL << 40)) return fail(c, IVR_ERR_UNSUPPORTED, "volume too large");
+    CK(c, cudaSetDevice(c->device));
+    ivr_volume *v = new ivr_volume();
+    v->ctx = c;
+    v->w = w; v->h = h; v->d = d; v->dtype = dtype;
+    v->full_bytes = (size_t) w * h * d * dtype_size(dtype);
+    int rc = dev_alloc(c, v->full_bytes, &v->d_full);
+    if (rc) { delete v; return rc; }
+    cudaError_t e = cudaMemcpy(v->d_full, host, v->full_bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && byteswap) e = launch_byteswap(v->d_full, (long long) w * h * d, (int) dtype_size(dtype), 0);
+    if (e != cudaSuccess) {
+        ivr_volume_free(v);
+        return cuda_fail(c, e, "volume upload");
+    }
+    rc = setup_bricks(v, 1, 1, 1, 0);
+    if (rc) { ivr_volume_free(v); return rc; }
+    *out = v;
+    return IVR_OK;
+}
+
+int ivr_volume_load_file(ivr_ctx *c, const char *path, int w, int h, int d, int dtype, int file_little_endian,
+                         ivr_volume **out)
+{
+    if (!c || !out) return IVR_ERR_INVALID;
+    *out = nullptr;
+    if (!path) return fail(c, IVR_ERR_INVALID, "null path");
+    if (w < 2 || h < 2 || d < 2 || (dtype != IVR_U8 && dtype != IVR_U16 && dtype != IVR_F32))
+        return fail(c, IVR_ERR_INVALID, "bad volume shape or dtype");
+    size_t bytes = (size_t) w * h * d * dtype_size(dtype);
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return fail(c, IVR_ERR_IO, "cannot open %s", path);
+    std::vector<unsigned char> buf(bytes);
+    size_t got = fread(buf.data(), 1, bytes, fp);
+    fclose(fp);
+    if (got != bytes) return fail(c, IVR_ERR_IO, "%s: read %zu of %zu bytes", path, got, bytes);
+    const uint16_t probe = 1;
+    const int host_little = *(const unsigned char *) &probe == 1;
+    return ivr_volume_load(c, buf.data(), w, h, d, dtype, (file_little_endian ? 1 : 0) != host_little, out);
+}
+
+int ivr_volume_free(ivr_volume *v)
+{
+    if (!v) return IVR_ERR_INVALID;
+    free_bricks(v);
+    dev_free(v->ctx, v->d_full, v->full_bytes);
+    delete v;
+    return IVR_OK;
+}
+
+int ivr_bricks_setup(ivr_volume *v, int py, int px, int pz, int overlap)
+{
+    if (!v) return IVR_ERR_INVALID;
+    return setup_bricks(v, py, px, pz, overlap);
+}
+
+int ivr_volume_minmax(ivr_volume *v, float *mn, float *mx)
+{
+    if (!v || !mn || !mx) return v ? fail(v->ctx, IVR_ERR_INVALID, "null output") : IVR_ERR_INVALID;
+    ivr_ctx *c = v->ctx;
+    if (!v->have_minmax) {
+        int parts = minmax_parts();
+        CK(c, launch_minmax(v->d_full, v->dtype, (long long) v->w * v->h * v->d, c->d_partial, parts, 0));
+        std::vector<float> h(2 * parts);
+        CK(c, cudaMemcpy(h.data(), c->d_partial, sizeof(float) * h.size(), cudaMemcpyDeviceToHost));
+        float lo = FLT_MAX, hi = -FLT_MAX;
+        for (int i = 0; i < parts; i++) {
+            lo = fminf(lo, h[2 * i]);
+            hi = fmaxf(hi, h[2 * i + 1]);
+        }
+        v->vmin = lo;
+        v->vmax = hi;
+        v->have_minmax = true;
+    }
+    *mn = v->vmin;
+    *mx = v->vmax;
+    return IVR_OK;
+}
+
+int ivr_volume_histogram(ivr_volume *v, int *hist, int hsize)
+{
+    if (!v || !hist || hsize < 1) return v ? fail(v->ctx, IVR_ERR_INVALID, "bad histogram output") : IVR_ERR_INVALID;
+    ivr_ctx *c = v->ctx;
+    float mn, mx;
+    int rc = ivr_volume_minmax(v, &mn, &mx);
+    if (rc) return rc;
+    int *d_hist = nullptr;
+    rc = dev_alloc(c, sizeof(int) * (size_t) hsize, (void **) &d_hist);
+    if (rc) return rc;
+    cudaError_t e = launch_histogram(v->d_full, v->dtype, (long long) v->w * v->h * v->d, mn, hsize, d_hist, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(hist, d_hist, sizeof(int) * (size_t) hsize, cudaMemcpyDeviceToHost);
+    dev_free(c, d_hist, sizeof(int) * (size_t) hsize);
+    if (e != cudaSuccess) return cuda_fail(c, e, "histogram");
+    return IVR_OK;
+}
+
+int ivr_tf_create(ivr_ctx *c, ivr_tf **out)
+{
+    if (!c || !out) return IVR_ERR_INVALID;
+    ivr_tf *t = new ivr_tf();
+    t->ctx = c;
+    *out = t;
+    return IVR_OK;
+}
+
+int ivr_tf_free(ivr_tf *t)
+{
+    if (!t) return IVR_ERR_INVALID;
+    dev_free(t->ctx, t->d_lut, sizeof(float4) * (size_t) t->cap);
+    dev_free(t->ctx, t->d_nzprefix, sizeof(int) * (size_t) (t->cap + 1));
+    delete t;
+    return IVR_OK;
+}
+
+int ivr_tf_set_lut(ivr_tf *t, const float *rgba, int n, int off, float scale, int mode)
+{
+    if (!t) return IVR_ERR_INVALID;
+    ivr_ctx *c = t->ctx;
+    if (mode < IVR_TF_SEISMIC || mode > IVR_TF_F2B) return fail(c, IVR_ERR_INVALID, "transfer function mode %d", mode);
+    if (mode != IVR_TF_RGBBLEND && (!rgba || n < 1)) return fail(c, IVR_ERR_INVALID, "empty LUT");
+    if (n > (1 << 24)) return fail(c, IVR_ERR_UNSUPPORTED, "LUT of %d entries", n);
+    if (mode != IVR_TF_F2B && scale != 1.0f) return fail(c, IVR_ERR_INVALID, "lut_scale applies to IVR_TF_F2B only");
+    if (!(scale > 0.0f)) return fail(c, IVR_ERR_INVALID, "lut_scale must be > 0");
+    if (n > t->cap) {
+        dev_free(c, t->d_lut, sizeof(float4) * (size_t) t->cap);
+        dev_free(c, t->d_nzprefix, sizeof(int) * (size_t) (t->cap + 1));
+        t->d_lut = nullptr;
+        t->d_nzprefix = nullptr;
+        t->cap = 0;
+        int rc = dev_alloc(c, sizeof(float4) * (size_t) n, (void **) &t->d_lut);
+        if (rc) return rc;
+        rc = dev_alloc(c, sizeof(int) * (size_t) (n + 1), (void **) &t->d_nzprefix);
+        if (rc) return rc;
+        t->cap = n;
+    }
+    t->n = n;
+    t->off = off;
+    t->scale = scale;
+    t->mode = mode;
+    if (n > 0) {
+        t->host.assign(rgba, rgba + 4 * (size_t) n);
+        std::vector<int> pre((size_t) n + 1, 0);
+        for (int i = 0; i < n; i++) pre[i + 1] = pre[i] + (rgba[4 * i + 3] != 0.0f ? 1 : 0);
+        CK(c, cudaMemcpy(t->d_lut, rgba, sizeof(float4) * (size_t) n, cudaMemcpyHostToDevice));
+        CK(c, cudaMemcpy(t->d_nzprefix, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice));
+    }
+    t->serial = ++c->tf_serial;
+    return IVR_OK;
+}
+
+int ivr_tf_set_colormap(ivr_tf *t, ivr_volume *v, int colormap, int mode)
+{
+    if (!t || !v) return IVR_ERR_INVALID;
+    ivr_ctx *c = t->ctx;
+    float mn, mx;
+    int rc = ivr_volume_minmax(v, &mn, &mx);
+    if (rc) return rc;
+    // initvolluts (main.c:1093, 1142, 1158-1179)
+    float span = (mx - mn) + 1;
+    if (!(span < (float) (1 << 24))) return fail(c, IVR_ERR_UNSUPPORTED, "value range %g needs too large a LUT", span);
+    int hsize = (int) span;
+    std::vector<float> lut(4 * (size_t) hsize);
+    build_colormap(colormap, lut.data(), hsize, mn, mx);
+    int off = (int) (mn + 0.5);
+    return ivr_tf_set_lut(t, lut.data(), hsize, off, 1.0f, mode);
+}
+
+int ivr_tf_get_lut(const ivr_tf *t, float *rgba, int n, int *lut_n, int *lut_off)
+{
+    if (!t) return IVR_ERR_INVALID;
+    if (lut_n) *lut_n = t->n;
+    if (lut_off) *lut_off = t->off;
+    if (rgba) {
+        int m = n < t->n ? n : t->n;
+        memcpy(rgba, t->host.data(), sizeof(float) * 4 * (size_t) m);
+    }
+    return IVR_OK;
+}
+
+int ivr_view_create(ivr_ctx *c, ivr_view **out)
+{
+    if (!c || !out) return IVR_ERR_INVALID;
+    ivr_view *v = new ivr_view();
+    v->ctx = c;
+    *out = v;
+    return IVR_OK;
+}
+
+int ivr_view_free(ivr_view *v)
+{
+    if (!v) return IVR_ERR_INVALID;
+    delete v;
+    return IVR_OK;
+}
+
+int ivr_set_view(ivr_view *view, ivr_volume *vol, const ivr_state *st, const ivr_render_params *p)
+{
+    if (!view) return IVR_ERR_INVALID;
+    ivr_ctx *c = view->ctx;
+    view->valid = false;
+    if (!vol || !st) return fail(c, IVR_ERR_INVALID, "null volume or state");
+    int rc = valid_params(c, p);
+    if (rc) return rc;
+    rc = build_frame(vol->w, vol->h, vol->d, vol->dtype, vol->bricks.data(), (int) vol->bricks.size(), *st, *p,
+                     view->f, view->info);
+    if (rc) return fail(c, rc, "view set-up failed (window %dx%d, tile %dx%d)", st->winwidth, st->winheight,
+                        p->tilew, p->tileh);
+    view->vol = vol;
+    view->p = *p;
+    view->st = *st;
+    view->valid = true;
+    return IVR_OK;
+}
+
+int ivr_view_info(const ivr_view *view, ivr_frame_info *info)
+{
+    if (!view || !info || !view->valid) return IVR_ERR_INVALID;
+    *info = view->info;
+    return IVR_OK;
+}
+
+int ivr_render(ivr_view *view, ivr_tf *tf, float *o32, uint8_t *o8, void *stream)
+{
+    if (!view) return IVR_ERR_INVALID;
+    return render_window(view, tf, 0, 0, view->info.vw, view->info.vh, -1, o32, o8, stream);
+}
+
+int ivr_render_tile(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, float *o32, uint8_t *o8, void *stream)
+{
+    return render_window(view, tf, x, y, w, h, -1, o32, o8, stream);
+}
+
+int ivr_render_brick(ivr_view *view, ivr_tf *tf, int brick, float *o32, void *stream)
+{
+    if (!view) return IVR_ERR_INVALID;
+    if (brick < 0 || brick >= view->info.nbricks) return fail(view->ctx, IVR_ERR_INVALID, "brick %d", brick);
+    return render_window(view, tf, 0, 0, view->info.vw, view->info.vh, brick, o32, nullptr, stream);
+}
+
+int ivr_render_host(ivr_view *view, ivr_volume *vol, ivr_tf *tf, const ivr_state *st, const ivr_render_params *p,
+                    uint8_t *host8, void *stream)
+{
+    if (!view || !host8) return view ? fail(view->ctx, IVR_ERR_INVALID, "null output") : IVR_ERR_INVALID;
+    ivr_ctx *c = view->ctx;
+    int rc = ivr_set_view(view, vol, st, p);
+    if (rc) return rc;
+    size_t bytes = (size_t) view->info.vw * view->info.vh * 4;
+    if (bytes > c->frame8_bytes) {
+        dev_free(c, c->d_frame8, c->frame8_bytes);
+        c->d_frame8 = nullptr;
+        c->frame8_bytes = 0;
+        rc = dev_alloc(c, bytes, (void **) &c->d_frame8);
+        if (rc) return rc;
+        c->frame8_bytes = bytes;
+    }
+    rc = ivr_render(view, tf, nullptr, (uint8_t *) c->d_frame8, stream);
+    if (rc) return rc;
+    CK(c, cudaMemcpyAsync(host8, c->d_frame8, bytes, cudaMemcpyDeviceToHost, (cudaStream_t) stream));
+    CK(c, cudaStreamSynchronize((cudaStream_t) stream));
+    return IVR_OK;
+}
+
+int ivr_composite(ivr_ctx *c, float *tilebuf, const float *rcolorbuf, int num, int w, int h, void *stream)
+{
+    if (!c) return IVR_ERR_INVALID;
+    if (!tilebuf || (num > 0 && !rcolorbuf) || num < 0 || w < 0 || h < 0)
+        return fail(c, IVR_ERR_INVALID, "bad composite arguments");
+    if (num == 0 || w == 0 || h == 0) return IVR_OK;
+    CK(c, launch_composite(tilebuf, rcolorbuf, num, (long long) w * h, (cudaStream_t) stream));
+    return IVR_OK;
+}
+
+int ivr_quantize(ivr_ctx *c, const float *in, uint8_t *out, long long n, void *stream)
+{
+    if (!c) return IVR_ERR_INVALID;
+    if (n < 0 || (n > 0 && (!in || !out))) return fail(c, IVR_ERR_INVALID, "bad quantize arguments");
+    if (n == 0) return IVR_OK;
+    CK(c, launch_quantize(in, out, n, (cudaStream_t) stream));
+    return IVR_OK;
+}
+
+}  // extern "C"

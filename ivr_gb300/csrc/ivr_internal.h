@@ -1,0 +1,91 @@
+// ivr_internal.h -- structures shared by the host code and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ivr_gpu.h"
+
+namespace ivr {
+
+constexpr int kMaxBricks = IVR_MAX_BRICKS;
+constexpr int kCell = 16;  // macrocell edge in voxels
+
+// One brick as the march kernels see it.  Geometry follows the reference's
+// per-rank AABB (main.c:552-618): bmin and w/h/d from the brick's world
+// extent, nx/ny/nz the local array dims including the halo.
+struct DevBrick {
+    const void *data;       // [nz][ny][nx] of the volume's dtype
+    int nx, ny, nz;
+    float bminx, bminy, bminz;
+    float w, h, d;          // aabb.w/h/d
+    float icx, icy, icz;    // CONFIG: core voxels per world unit
+    float dconst[6];        // clip-plane constants of this brick
+    int istrt, istop, jstrt, jstop;  // pixel rect (createlocalimage)
+    float dir0x, dir0y, dir0z;       // REF: ray direction at (istrt, jstrt)
+    const uint8_t *empty;   // per-macrocell "zero opacity" flags, or null
+    int mcx, mcy, mcz;      // macrocell grid dims
+};
+
+// Everything one launch needs, passed by value as a __grid_constant__.
+struct FrameDesc {
+    int vw, vh;              // viewport
+    int nb;                  // bricks
+    int preset, tf_mode, dtype;
+    float origx, origy, origz;
+    float incrix, incriy, incriz;
+    float incrjx, incrjy, incrjz;
+    float ctm[9];            // CONFIG ray directions: ctm * (u, v, 5)
+    float left, bottom, du, dv, eyen;
+    float step;              // REF: ray-parameter step; CONFIG: world step
+    int max_samples;         // 0 = unbounded
+    float term_alpha;
+    float alpha;             // opacity scale (STATE.alpha)
+    const float4 *lut;
+    int lut_n, lut_off;
+    float lut_scale;
+    float gdconst[6];        // CONFIG: the clipped global box
+    int out_x, out_y, out_w, out_h;  // output window in viewport pixels
+    int single;              // >= 0: render only this brick (no compositing)
+    unsigned long long *counters;    // [0] executed samples (nullable)
+    int order[kMaxBricks];   // near -> far
+    DevBrick b[kMaxBricks];
+};
+
+// Host-side brick record (device array + geometry that does not depend on
+// the view).
+struct HostBrick {
+    int lw, lh, ld;     // local dims incl. halo
+    int cw, ch, cd;     // core dims
+    int sx, sy, sz;     // start index in the global volume
+    int col, row, slab;
+    float bminx, bminy, bminz, bmaxx, bmaxy, bmaxz;
+    float w, h, d;
+    void *data;         // device
+    bool owns;          // false when it aliases the full volume
+    float *mc_minmax;   // device [mcz][mcy][mcx][2]
+    uint8_t *empty;     // device [mcz][mcy][mcx]
+    int mcx, mcy, mcz;
+};
+
+size_t dtype_size(int dtype);
+
+// kernels (ivr_kernels.cu)
+cudaError_t launch_byteswap(void *data, long long n, int elem, cudaStream_t s);
+cudaError_t launch_gather_brick(const void *src, int gw, int gh, int gd, void *dst, int sx, int sy, int sz,
+                                int lw, int lh, int ld, int elem, cudaStream_t s);
+cudaError_t launch_minmax(const void *data, int dtype, long long n, float *partial, int nparts, cudaStream_t s);
+cudaError_t launch_histogram(const void *data, int dtype, long long n, float mn, int hsize, int *hist,
+                             cudaStream_t s);
+cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int nz, float *mc, int mcx, int mcy,
+                              int mcz, cudaStream_t s);
+cudaError_t launch_empty_flags(const float *mc, int ncell, const int *nzprefix, int lut_n, int lut_off,
+                               float lut_scale, uint8_t *empty, cudaStream_t s);
+cudaError_t launch_composite(float *dst, const float *src, int num, long long npix, cudaStream_t s);
+cudaError_t launch_quantize(const float *in, uint8_t *out, long long n, cudaStream_t s);
+int minmax_parts();
+
+// march (ivr_march.cu)
+cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s);
+
+}  // namespace ivr

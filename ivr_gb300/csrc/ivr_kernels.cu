@@ -1,0 +1,262 @@
+// ivr_kernels.cu -- the kernels around the march: byte swap, brick gather,
+// min/max + histogram (initvolluts), macrocell min/max and per-TF empty
+// flags, sort-last compositing (compositetiles) and RGBA8 quantisation.
+// Compiled with -fmad=false like the march.
+#include <float.h>
+#include <stdint.h>
+
+#include "ivr_internal.h"
+
+namespace ivr {
+namespace {
+
+constexpr int kSms = 152;
+
+int grid_for(long long n, int threads, int per_sm = 8)
+{
+    long long g = (n + threads - 1) / threads;
+    long long cap = (long long) kSms * per_sm;
+    return (int) (g < cap ? (g < 1 ? 1 : g) : cap);
+}
+
+template <typename T> __device__ __forceinline__ float tof(T v) { return (float) v; }
+
+__device__ __forceinline__ float load_any(const void *p, int dtype, long long i)
+{
+    switch (dtype) {
+    case IVR_U8: return (float) __ldg(reinterpret_cast<const uint8_t *>(p) + i);
+    case IVR_U16: return (float) __ldg(reinterpret_cast<const uint16_t *>(p) + i);
+    default: return __ldg(reinterpret_cast<const float *>(p) + i);
+    }
+}
+
+__global__ void byteswap16_kernel(uint16_t *p, long long n)
+{
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+        p[i] = (uint16_t) ((p[i] >> 8) | (p[i] << 8));
+}
+
+// BYTESWAP_FP (sysutil.h:121-133): byte order reversed
+__global__ void byteswap32_kernel(uint32_t *p, long long n)
+{
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+        p[i] = __byte_perm(p[i], 0, 0x0123);
+}
+
+// readfromfile (main.c:1254-1265): brick [sz..sz+ld) x [sy..sy+lh) x
+// [sx..sx+lw) of the global volume into a dense [ld][lh][lw] array.
+template <typename T>
+__global__ void gather_kernel(const T *__restrict__ src, int gw, int gh, T *__restrict__ dst, int sx, int sy,
+                              int sz, int lw, int lh, long long n)
+{
+    for (long long o = blockIdx.x * (long long) blockDim.x + threadIdx.x; o < n; o += (long long) gridDim.x * blockDim.x) {
+        int x = (int) (o % lw);
+        long long r = o / lw;
+        int y = (int) (r % lh);
+        int z = (int) (r / lh);
+        dst[o] = src[((long long) (sz + z) * gh + (sy + y)) * gw + (sx + x)];
+    }
+}
+
+__global__ void minmax_kernel(const void *data, int dtype, long long n, float *partial)
+{
+    float lo = FLT_MAX, hi = -FLT_MAX;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        float v = load_any(data, dtype, i);
+        lo = fminf(lo, v);
+        hi = fmaxf(hi, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    __shared__ float slo[32], shi[32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { slo[w] = lo; shi[w] = hi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int) (blockDim.x >> 5); k++) { lo = fminf(lo, slo[k]); hi = fmaxf(hi, shi[k]); }
+        partial[2 * blockIdx.x] = lo;
+        partial[2 * blockIdx.x + 1] = hi;
+    }
+}
+
+// histogram (mathutil.c:459-467): bin (int)(v - min); privatised in shared
+// memory when the bins fit.
+constexpr int kSmemBins = 12288;
+__global__ void hist_smem_kernel(const void *data, int dtype, long long n, float mn, int hsize, int *hist)
+{
+    __shared__ int sh[kSmemBins];
+    for (int b = threadIdx.x; b < hsize; b += blockDim.x) sh[b] = 0;
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        int b = (int) (load_any(data, dtype, i) - mn);
+        if (b >= 0 && b < hsize) atomicAdd(&sh[b], 1);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < hsize; b += blockDim.x)
+        if (sh[b]) atomicAdd(&hist[b], sh[b]);
+}
+__global__ void hist_global_kernel(const void *data, int dtype, long long n, float mn, int hsize, int *hist)
+{
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        int b = (int) (load_any(data, dtype, i) - mn);
+        if (b >= 0 && b < hsize) atomicAdd(&hist[b], 1);
+    }
+}
+
+// Macrocell min/max: cell (cx,cy,cz) spans voxels [c*16, min(c*16+16, n-1)]
+// per axis -- its 16 cells plus the +1 layer a trilinear sample in the cell
+// also reads.  One block per cell.
+__global__ void macrocell_kernel(const void *data, int dtype, int nx, int ny, int nz, float *mc, int mcx, int mcy)
+{
+    const int cid = blockIdx.x;
+    const int cx = cid % mcx, cy = (cid / mcx) % mcy, cz = cid / (mcx * mcy);
+    const int x0 = cx * kCell, y0 = cy * kCell, z0 = cz * kCell;
+    const int x1 = min(x0 + kCell, nx - 1), y1 = min(y0 + kCell, ny - 1), z1 = min(z0 + kCell, nz - 1);
+    const int ex = x1 - x0 + 1, ey = y1 - y0 + 1, ez = z1 - z0 + 1;
+    float lo = FLT_MAX, hi = -FLT_MAX;
+    const int tot = ex * ey * ez;
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+        int x = t % ex, r = t / ex;
+        int y = r % ey, z = r / ey;
+        float v = load_any(data, dtype, ((long long) (z0 + z) * ny + (y0 + y)) * nx + (x0 + x));
+        lo = fminf(lo, v);
+        hi = fmaxf(hi, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    __shared__ float slo[32], shi[32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { slo[w] = lo; shi[w] = hi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int) (blockDim.x >> 5); k++) { lo = fminf(lo, slo[k]); hi = fmaxf(hi, shi[k]); }
+        mc[2 * cid] = lo;
+        mc[2 * cid + 1] = hi;
+    }
+}
+
+// A cell is empty when no LUT entry its samples can index has non-zero
+// opacity.  Samples lie in [min, max] of the cell's voxels up to rounding,
+// so the index range is widened by one on each side.  nzprefix[i] = number
+// of entries in [0, i) with non-zero opacity.
+__global__ void empty_kernel(const float *mc, int ncell, const int *nzprefix, int lut_n, int lut_off,
+                             float lut_scale, uint8_t *empty)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
+        int lo = (int) (mc[2 * c] * lut_scale) - 1 - lut_off;
+        int hi = (int) (mc[2 * c + 1] * lut_scale) + 1 - lut_off;
+        lo = min(max(lo, 0), lut_n - 1);
+        hi = min(max(hi, 0), lut_n - 1);
+        empty[c] = (nzprefix[hi + 1] - nzprefix[lo]) == 0 ? 1 : 0;
+    }
+}
+
+// compositetiles (main.c:1203-1218)
+__global__ void composite_kernel(float4 *dst, const float4 *__restrict__ src, int num, long long npix)
+{
+    for (long long p = blockIdx.x * (long long) blockDim.x + threadIdx.x; p < npix; p += (long long) gridDim.x * blockDim.x) {
+        float4 d = dst[p];
+        for (int k = num - 1; k >= 0; k--) {
+            float4 s = __ldg(src + (long long) k * npix + p);
+            d.z = s.z + (1.0f - s.w) * d.z;
+            d.y = s.y + (1.0f - s.w) * d.y;
+            d.x = s.x + (1.0f - s.w) * d.x;
+            d.w = s.w + (1.0f - s.w) * d.w;
+        }
+        dst[p] = d;
+    }
+}
+
+// (uint8)(v*255 + 0.5) for v clamped to [0,1], computed exactly in integers
+// (see q8 in ivr_march.cu).
+__device__ __forceinline__ unsigned q8k(float v)
+{
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 1.0f) return 255u;
+    unsigned bits = __float_as_uint(v);
+    int e = (int) (bits >> 23);
+    if (e == 0) return 0u;
+    unsigned long long m = (bits & 0x7fffffu) | 0x800000u;
+    int s = 150 - e;
+    if (s >= 34) return 0u;
+    return (unsigned) ((255ull * m + (1ull << (s - 1))) >> s);
+}
+
+__global__ void quantize_kernel(const float *__restrict__ in, uint8_t *__restrict__ out, long long n)
+{
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+        out[i] = (uint8_t) q8k(in[i]);
+}
+
+}  // namespace
+
+size_t dtype_size(int dtype) { return dtype == IVR_U8 ? 1 : dtype == IVR_U16 ? 2 : 4; }
+
+int minmax_parts() { return kSms * 4; }
+
+cudaError_t launch_byteswap(void *data, long long n, int elem, cudaStream_t s)
+{
+    if (n <= 0 || elem == 1) return cudaSuccess;
+    if (elem == 2) byteswap16_kernel<<<grid_for(n, 256), 256, 0, s>>>((uint16_t *) data, n);
+    else byteswap32_kernel<<<grid_for(n, 256), 256, 0, s>>>((uint32_t *) data, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_brick(const void *src, int gw, int gh, int gd, void *dst, int sx, int sy, int sz, int lw,
+                                int lh, int ld, int elem, cudaStream_t s)
+{
+    (void) gd;
+    long long n = (long long) lw * lh * ld;
+    int g = grid_for(n, 256);
+    if (elem == 1) gather_kernel<uint8_t><<<g, 256, 0, s>>>((const uint8_t *) src, gw, gh, (uint8_t *) dst, sx, sy, sz, lw, lh, n);
+    else if (elem == 2) gather_kernel<uint16_t><<<g, 256, 0, s>>>((const uint16_t *) src, gw, gh, (uint16_t *) dst, sx, sy, sz, lw, lh, n);
+    else gather_kernel<uint32_t><<<g, 256, 0, s>>>((const uint32_t *) src, gw, gh, (uint32_t *) dst, sx, sy, sz, lw, lh, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_minmax(const void *data, int dtype, long long n, float *partial, int nparts, cudaStream_t s)
+{
+    minmax_kernel<<<nparts, 256, 0, s>>>(data, dtype, n, partial);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_histogram(const void *data, int dtype, long long n, float mn, int hsize, int *hist, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(int) * (size_t) hsize, s);
+    if (e != cudaSuccess) return e;
+    if (hsize <= kSmemBins) hist_smem_kernel<<<grid_for(n, 512, 2), 512, 0, s>>>(data, dtype, n, mn, hsize, hist);
+    else hist_global_kernel<<<grid_for(n, 256), 256, 0, s>>>(data, dtype, n, mn, hsize, hist);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int nz, float *mc, int mcx, int mcy,
+                              int mcz, cudaStream_t s)
+{
+    macrocell_kernel<<<mcx * mcy * mcz, 128, 0, s>>>(data, dtype, nx, ny, nz, mc, mcx, mcy);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_empty_flags(const float *mc, int ncell, const int *nzprefix, int lut_n, int lut_off,
+                               float lut_scale, uint8_t *empty, cudaStream_t s)
+{
+    empty_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mc, ncell, nzprefix, lut_n, lut_off, lut_scale, empty);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_composite(float *dst, const float *src, int num, long long npix, cudaStream_t s)
+{
+    composite_kernel<<<grid_for(npix, 256), 256, 0, s>>>((float4 *) dst, (const float4 *) src, num, npix);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_quantize(const float *in, uint8_t *out, long long n, cudaStream_t s)
+{
+    quantize_kernel<<<grid_for(n, 256), 256, 0, s>>>(in, out, n);
+    return cudaGetLastError();
+}
+
+}  // namespace ivr

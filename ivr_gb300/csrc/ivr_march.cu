@@ -1,0 +1,463 @@
+// ivr_march.cu -- the per-ray march: ray setup, slab test, sample lattice,
+// trilinear reconstruction, transfer function, brick compositing, RGBA
+// stores.  One thread per ray; a warp covers an 8x4 screen tile.
+//
+// Compiled with -fmad=false: every float multiply and add is rounded on its
+// own, as in the reference's C, unless written as fmaf() here.  With IEEE
+// division and square root (no fast-math) the REF preset reproduces the
+// reference's arithmetic operation for operation.
+#include <float.h>
+#include <stdint.h>
+
+#include "ivr_internal.h"
+
+namespace ivr {
+namespace {
+
+constexpr int kBlockX = 16;  // pixels per block: 2x2 warps of 8x4
+constexpr int kBlockY = 8;
+constexpr int kThreads = 128;
+
+template <int DT> struct VoxT;
+template <> struct VoxT<IVR_U8> { using T = uint8_t; };
+template <> struct VoxT<IVR_U16> { using T = uint16_t; };
+template <> struct VoxT<IVR_F32> { using T = float; };
+
+template <int DT>
+__device__ __forceinline__ float vload(const void *p, long long i)
+{
+    return (float) __ldg(reinterpret_cast<const typename VoxT<DT>::T *>(p) + i);
+}
+
+// getrayintersect (ray.c:276-318).  All six planes are visited: once
+// tin >= tout no later plane can make it a hit, so skipping the reference's
+// early loop exit changes nothing.
+__device__ __forceinline__ bool ray_box(const float *dc, float ox, float oy, float oz, float dx, float dy,
+                                        float dz, float &tin, float &tout)
+{
+    tin = -FLT_MAX;
+    tout = FLT_MAX;
+#pragma unroll
+    for (int p = 0; p < 6; p++) {
+        const int axis = p >> 1;
+        const float nrm = (p & 1) ? 1.0f : -1.0f;
+        const float nx = axis == 0 ? nrm : 0.0f, ny = axis == 1 ? nrm : 0.0f, nz = axis == 2 ? nrm : 0.0f;
+        float numer = dc[p] - (nx * ox + ny * oy + nz * oz);
+        float denom = nx * dx + ny * dy + nz * dz;
+        if (tin < tout) {
+            if (denom == 0.0f) {
+                if (numer < 0.0f) tin = tout + 1.0f;
+            } else {
+                float thit = numer / denom;
+                if (denom > 0.0f) tout = fminf(tout, thit);
+                else tin = fmaxf(tin, thit);
+            }
+        }
+    }
+    return tin < tout && (tin > 0.0f || tout > 0.0f);
+}
+
+// getlinearsample (ray.c:87-181, non-BGQ branch), quirks included: the
+// weights are scaled by the cell size squared, and the x weight blends the
+// +1 row (y) neighbour.  x + fabs(min.x) is a double sum in the reference,
+// which rounds to the same float as this float sum.
+template <int DT>
+__device__ __forceinline__ float sample_ref(const DevBrick &b, float x, float y, float z)
+{
+    const int vw = b.nx, vh = b.ny, vd = b.nz;
+    float ratio = (x - b.bminx) / b.w;
+    int j = (int) ((float) vw * ratio);
+    ratio = (y - b.bminy) / b.h;
+    int i = (int) ((float) vh * ratio);
+    ratio = (z - b.bminz) / b.d;
+    int k = (int) ((float) vd * ratio);
+    i = min(i, vh - 2);
+    j = min(j, vw - 2);
+    k = min(k, vd - 2);
+    i = max(i, 0);  // no lower clamp in the reference; guards memory only
+    j = max(j, 0);
+    k = max(k, 0);
+    const long long row = vw, slab = (long long) vw * vh;
+    const long long p = k * slab + i * row + j;
+    float v000 = vload<DT>(b.data, p);
+    float v100 = vload<DT>(b.data, p + row);
+    float v010 = vload<DT>(b.data, p + 1);
+    float v001 = vload<DT>(b.data, p + slab);
+    float v101 = vload<DT>(b.data, p + row + slab);
+    float v011 = vload<DT>(b.data, p + 1 + slab);
+    float v110 = vload<DT>(b.data, p + row + 1);
+    float v111 = vload<DT>(b.data, p + row + 1 + slab);
+    float xp = x + fabsf(b.bminx), yp = y + fabsf(b.bminy), zp = z + fabsf(b.bminz);
+    float x0 = ((float) j * b.w) / (float) vw;
+    float y0 = ((float) i * b.h) / (float) vh;
+    float z0 = ((float) k * b.d) / (float) vd;
+    float xd = (fabsf(xp - x0) * b.w) / (float) vw;
+    float yd = (fabsf(yp - y0) * b.h) / (float) vh;
+    float zd = (fabsf(zp - z0) * b.d) / (float) vd;
+    float c00 = v000 * (1.0f - xd) + v100 * xd;
+    float c10 = v010 * (1.0f - xd) + v110 * xd;
+    float c01 = v001 * (1.0f - xd) + v101 * xd;
+    float c11 = v011 * (1.0f - xd) + v111 * xd;
+    float c0 = c00 * (1.0f - yd) + c10 * yd;
+    float c1 = c01 * (1.0f - yd) + c11 * yd;
+    return c0 * (1.0f - zd) + c1 * zd;
+}
+
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return fmaf(t, b - a, a); }
+
+// CONFIG sampler: trilinear with voxel values at cell corners (the
+// reference's index convention; the halo sits on the high side), clamp to
+// edge.
+template <int DT>
+__device__ __forceinline__ float sample_cfg(const DevBrick &b, float x, float y, float z)
+{
+    const int nx = b.nx, ny = b.ny, nz = b.nz;
+    float ux = (x - b.bminx) * b.icx;
+    float uy = (y - b.bminy) * b.icy;
+    float uz = (z - b.bminz) * b.icz;
+    int j = min(max((int) floorf(ux), 0), nx - 2);
+    int i = min(max((int) floorf(uy), 0), ny - 2);
+    int k = min(max((int) floorf(uz), 0), nz - 2);
+    float fx = fminf(fmaxf(ux - (float) j, 0.0f), 1.0f);
+    float fy = fminf(fmaxf(uy - (float) i, 0.0f), 1.0f);
+    float fz = fminf(fmaxf(uz - (float) k, 0.0f), 1.0f);
+    const long long sy = nx, sz = (long long) nx * ny;
+    const long long p = k * sz + i * sy + j;
+    float c00 = lerpf(vload<DT>(b.data, p), vload<DT>(b.data, p + 1), fx);
+    float c10 = lerpf(vload<DT>(b.data, p + sy), vload<DT>(b.data, p + sy + 1), fx);
+    float c01 = lerpf(vload<DT>(b.data, p + sz), vload<DT>(b.data, p + sz + 1), fx);
+    float c11 = lerpf(vload<DT>(b.data, p + sz + sy), vload<DT>(b.data, p + sz + sy + 1), fx);
+    float c0 = lerpf(c00, c10, fy);
+    float c1 = lerpf(c01, c11, fy);
+    return lerpf(c0, c1, fz);
+}
+
+__device__ __forceinline__ float4 lut_at(const FrameDesc &f, int idx)
+{
+    idx = min(max(idx, 0), f.lut_n - 1);
+    return __ldg(f.lut + idx);
+}
+
+// raycast (ray.c:59-85) + getsamplesonray (ray.c:239-273) + one transfer
+// function of transferfuncs.c:24-199.  Samples are computed in the order the
+// transfer function consumes them (ascending or descending) instead of
+// being stored.  Returns (r, g, b, a).
+template <int DT, int TF>
+__device__ float4 raycast_ref(const FrameDesc &f, const DevBrick &b, float dx, float dy, float dz,
+                              unsigned long long &nexec)
+{
+    float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float tin, tout;
+    if (!ray_box(b.dconst, f.origx, f.origy, f.origz, dx, dy, dz, tin, tout)) return c;
+    const float dt = f.step;
+    int iend = (int) (1.0f + (tout - tin) / dt + 0.5f);
+    if (f.max_samples > 0 && iend > f.max_samples) iend = f.max_samples;
+    if (iend <= 0) return c;
+    nexec += (unsigned long long) iend;
+    const float ox = f.origx, oy = f.origy, oz = f.origz;
+    const float myalpha = f.alpha;
+    auto sample = [&](int i) {
+        float t = tin + ((float) i * dt);
+        return sample_ref<DT>(b, dx * t + ox, dy * t + oy, dz * t + oz);
+    };
+    if (TF == IVR_TF_MED) {  // transferfuncs.c:24-68
+        for (int i = 0; i < iend; ++i) {
+            float4 e = lut_at(f, (int) sample(i) - f.lut_off);
+            c.z = ((double) e.z < 0.8) ? fmaxf(e.z, c.z) : c.z;
+            c.y = ((double) e.y < 0.8) ? fmaxf(e.y, c.y) : c.y;
+            c.x = ((double) e.x < 0.8) ? fmaxf(e.x, c.x) : c.x;
+            c.w = e.w * myalpha;
+        }
+    } else if (TF == IVR_TF_BLEND) {  // transferfuncs.c:70-83 (no lutoffset)
+        for (int i = 0; i < iend; ++i) {
+            float4 e = lut_at(f, (int) sample(i));
+            float al = e.w;
+            c.z = al * e.z + (1.0f - al) * c.z;
+            c.y = al * e.y + (1.0f - al) * c.y;
+            c.x = al * e.x + (1.0f - al) * c.x;
+            c.w = al * myalpha;
+        }
+    } else if (TF == IVR_TF_SEISMIC2 || TF == IVR_TF_CHEM) {  // transferfuncs.c:109-168
+        for (int i = iend - 1; i >= 0; i--) {
+            int idx = (int) sample(i) - f.lut_off;
+            if (idx < 0) idx = 0;
+            if (TF == IVR_TF_SEISMIC2 && idx > f.lut_n - 1) idx = f.lut_n - 1;
+            float4 e = lut_at(f, idx);
+            float al = e.w * myalpha;
+            float oma = 1.0f - al;
+            c.z = oma * c.z + al * e.z;
+            c.y = oma * c.y + al * e.y;
+            c.x = oma * c.x + al * e.x;
+            c.w = al + oma * c.w;
+            if (c.w > 1.0f) c.w = 1.0f;
+        }
+    } else if (TF == IVR_TF_RGBBLEND) {  // transferfuncs.c:170-200
+        for (int i = iend - 1; i >= 0; i--) {
+            unsigned u = __float_as_uint(sample(i));
+            float r = 1.0f / 255.0f * (float) ((u >> 24) & 0xff);
+            float g = 1.0f / 255.0f * (float) ((u >> 16) & 0xff);
+            float bl = 1.0f / 255.0f * (float) ((u >> 8) & 0xff);
+            float al = myalpha;
+            float oma = 1.0f - al;
+            c.z = oma * c.z + al * bl;
+            c.y = oma * c.y + al * g;
+            c.x = oma * c.x + al * r;
+            c.w = al + oma * c.w;
+            if (c.w > 1.0f) c.w = 1.0f;
+        }
+    } else {  // IVR_TF_SEISMIC, transferfuncs.c:86-107
+        for (int i = 0; i < iend; ++i) {
+            float4 e = lut_at(f, (int) sample(i) - f.lut_off);
+            c.z = ((double) e.z > 0.65 && e.z < 1.0f) ? 0.6f : c.z;
+            c.y = ((double) e.y > 0.65 && e.y < 1.0f) ? 0.0f : c.y;
+            c.x = ((double) e.x > 0.65 && e.x < 1.0f) ? 0.0f : c.x;
+            c.z = ((double) e.z > 0.5 && e.z < 0.65f) ? 0.9f : c.z;
+            c.y = ((double) e.y > 0.5 && e.y < 0.65f) ? 0.9f : c.y;
+            c.x = ((double) e.x > 0.5 && e.x < 0.65f) ? 0.9f : c.x;
+            c.z = ((double) e.z > 0.3 && e.z < 0.5f) ? 0.0f : c.z;
+            c.y = ((double) e.y > 0.3 && e.y < 0.5f) ? 0.0f : c.y;
+            c.x = ((double) e.x > 0.3 && e.x < 0.5f) ? 0.6f : c.x;
+            c.w = 1.0f * myalpha;
+        }
+    }
+    return c;
+}
+
+// compositetiles (main.c:1206-1215): d = s + (1 - s.a) * d
+__device__ __forceinline__ float4 over(float4 s, float4 d)
+{
+    d.z = s.z + (1.0f - s.w) * d.z;
+    d.y = s.y + (1.0f - s.w) * d.y;
+    d.x = s.x + (1.0f - s.w) * d.x;
+    d.w = s.w + (1.0f - s.w) * d.w;
+    return d;
+}
+
+// (uint8)(v*255 + 0.5) for v in [0,1], exact: for v = m * 2^(e-150) the
+// value is floor((255 m + 2^(s-1)) / 2^s) with s = 150 - e.
+__device__ __forceinline__ unsigned q8(float v)
+{
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 1.0f) return 255u;
+    unsigned bits = __float_as_uint(v);
+    int e = (int) (bits >> 23);
+    if (e == 0) return 0u;  // subnormal: far below 1/510
+    unsigned long long m = (bits & 0x7fffffu) | 0x800000u;
+    int s = 150 - e;
+    if (s >= 34) return 0u;
+    return (unsigned) ((255ull * m + (1ull << (s - 1))) >> s);
+}
+
+__device__ __forceinline__ bool in_rect(const DevBrick &b, int i, int j)
+{
+    return i >= b.istrt && i < b.istop && j >= b.jstrt && j < b.jstop;
+}
+
+// CONFIG lattice: t_i = fmaf(i, dt, t0).
+__device__ __forceinline__ float cfg_t(float t0, float dt, int i) { return fmaf((float) i, dt, t0); }
+__device__ __forceinline__ int cfg_first_ge(float t0, float dt, float a)
+{
+    if (!(a > t0)) return 0;
+    float q = (a - t0) / dt;
+    int i = q > 1.0e9f ? 1000000000 : (int) q;
+    while (i > 0 && cfg_t(t0, dt, i - 1) >= a) i--;
+    while (cfg_t(t0, dt, i) < a) i++;
+    return i;
+}
+
+// Is macrocell (ci,cj,ck) of a brick transparent under the current TF?
+__device__ __forceinline__ bool cell_empty(const DevBrick &b, int ci, int cj, int ck)
+{
+    return b.empty[((long long) ck * b.mcy + ci) * b.mcx + cj] != 0;
+}
+
+// One brick of the CONFIG march: samples tin_k <= t_i < tout_k of the ray's
+// lattice, front-to-back into (c, a).  With a macrocell grid, samples whose
+// cell is transparent are stepped over in one jump: every sample actually
+// taken is computed exactly as without skipping, and a skipped sample would
+// have had zero opacity, which leaves (c, a) unchanged.
+template <int DT, bool SKIP>
+__device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float dy, float dz, float t0,
+                          float dt, float4 &acc, bool &done, unsigned long long &nexec)
+{
+    float tin, tout;
+    if (!ray_box(b.dconst, f.origx, f.origy, f.origz, dx, dy, dz, tin, tout)) return;
+    int i0 = cfg_first_ge(t0, dt, tin);
+    int i1 = cfg_first_ge(t0, dt, tout);
+    const float ox = f.origx, oy = f.origy, oz = f.origz;
+    const float opac = f.alpha, term = f.term_alpha;
+    for (int i = i0; i < i1; i++) {
+        float t = cfg_t(t0, dt, i);
+        float x = fmaf(dx, t, ox), y = fmaf(dy, t, oy), z = fmaf(dz, t, oz);
+        if (SKIP) {
+            // cell of this sample in the brick's voxel index space
+            float ux = (x - b.bminx) * b.icx, uy = (y - b.bminy) * b.icy, uz = (z - b.bminz) * b.icz;
+            int j = min(max((int) floorf(ux), 0), b.nx - 2);
+            int ii = min(max((int) floorf(uy), 0), b.ny - 2);
+            int k = min(max((int) floorf(uz), 0), b.nz - 2);
+            int cj = j / kCell, ci = ii / kCell, ck = k / kCell;
+            if (cell_empty(b, ci, cj, ck)) {
+                // exit parameter of this cell's box along the ray, in world
+                // coordinates; jump to one sample before it (the sample there
+                // is re-checked, so rounding in the exit never skips a
+                // non-empty sample)
+                float lo_x = b.bminx + (float) (cj * kCell) / b.icx, hi_x = b.bminx + (float) ((cj + 1) * kCell) / b.icx;
+                float lo_y = b.bminy + (float) (ci * kCell) / b.icy, hi_y = b.bminy + (float) ((ci + 1) * kCell) / b.icy;
+                float lo_z = b.bminz + (float) (ck * kCell) / b.icz, hi_z = b.bminz + (float) ((ck + 1) * kCell) / b.icz;
+                float tx = dx > 0.0f ? (hi_x - ox) / dx : (dx < 0.0f ? (lo_x - ox) / dx : FLT_MAX);
+                float ty = dy > 0.0f ? (hi_y - oy) / dy : (dy < 0.0f ? (lo_y - oy) / dy : FLT_MAX);
+                float tz = dz > 0.0f ? (hi_z - oz) / dz : (dz < 0.0f ? (lo_z - oz) / dz : FLT_MAX);
+                float texit = fminf(tx, fminf(ty, tz));
+                int inext = (int) ((texit - t0) / dt) - 1;
+                if (inext > i) i = min(inext, i1) - 1;  // loop ++ lands on inext
+                continue;
+            }
+        }
+        float s = sample_cfg<DT>(b, x, y, z);
+        nexec++;
+        float4 e = lut_at(f, (int) (s * f.lut_scale) - f.lut_off);
+        float al = e.w * opac;
+        float wgt = (1.0f - acc.w) * al;
+        acc.x = fmaf(wgt, e.x, acc.x);
+        acc.y = fmaf(wgt, e.y, acc.y);
+        acc.z = fmaf(wgt, e.z, acc.z);
+        acc.w = acc.w + wgt;
+        if (acc.w >= term) {
+            done = true;
+            return;
+        }
+    }
+}
+
+__device__ __forceinline__ void count_exec(const FrameDesc &f, unsigned long long nexec)
+{
+    if (f.counters == nullptr) return;
+    unsigned mask = __activemask();
+    for (int o = 16; o > 0; o >>= 1) nexec += __shfl_xor_sync(mask, nexec, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(f.counters, nexec);
+}
+
+__device__ __forceinline__ void pixel_of(const FrameDesc &f, int &i, int &j, int &oi, int &oj)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    oj = blockIdx.x * kBlockX + (warp & 1) * 8 + (lane & 7);
+    oi = blockIdx.y * kBlockY + (warp >> 1) * 4 + (lane >> 3);
+    j = f.out_x + oj;
+    i = f.out_y + oi;
+}
+
+template <int DT, int TF>
+__global__ void __launch_bounds__(kThreads) march_ref_kernel(const __grid_constant__ FrameDesc f, float4 *out32,
+                                                             uchar4 *out8)
+{
+    int i, j, oi, oj;
+    pixel_of(f, i, j, oi, oj);
+    if (oj >= f.out_w || oi >= f.out_h) return;
+    float4 d = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    unsigned long long nexec = 0;
+    if (i < f.vh && j < f.vw) {
+        // far -> near over of per-brick colours; each brick casts its own ray
+        // with the sequential column increments of createlocalimage
+        // (main.c:986-999)
+        for (int s = f.nb - 1; s >= 0; s--) {
+            const int k = f.order[s];
+            if (f.single >= 0 && k != f.single) continue;
+            const DevBrick &b = f.b[k];
+            if (!in_rect(b, i, j)) continue;
+            const float fi = (float) (i - b.istrt);
+            float dx = b.dir0x + f.incrix * fi, dy = b.dir0y + f.incriy * fi, dz = b.dir0z + f.incriz * fi;
+            for (int c = b.jstrt; c <= j; c++) {
+                dx += f.incrjx;
+                dy += f.incrjy;
+                dz += f.incrjz;
+            }
+            float4 cs = raycast_ref<DT, TF>(f, b, dx, dy, dz, nexec);
+            d = over(cs, d);
+        }
+    }
+    const long long o = (long long) oi * f.out_w + oj;
+    if (out32) out32[o] = d;
+    if (out8) out8[o] = make_uchar4(q8(d.x), q8(d.y), q8(d.z), q8(d.w));
+    count_exec(f, nexec);
+}
+
+template <int DT, bool SKIP>
+__global__ void __launch_bounds__(kThreads) march_cfg_kernel(const __grid_constant__ FrameDesc f, float4 *out32,
+                                                             uchar4 *out8)
+{
+    int i, j, oi, oj;
+    pixel_of(f, i, j, oi, oj);
+    if (oj >= f.out_w || oi >= f.out_h) return;
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    unsigned long long nexec = 0;
+    bool any = false;
+    if (i < f.vh && j < f.vw)
+        for (int k = 0; k < f.nb; k++) any |= in_rect(f.b[k], i, j);
+    if (any) {
+        // ctm * (u, v, 5) at the pixel centre
+        float u = f.left + ((float) j + 0.5f) * f.du;
+        float v = f.bottom + ((float) i + 0.5f) * f.dv;
+        float dx = f.ctm[0] * u + f.ctm[1] * v + f.ctm[2] * f.eyen;
+        float dy = f.ctm[3] * u + f.ctm[4] * v + f.ctm[5] * f.eyen;
+        float dz = f.ctm[6] * u + f.ctm[7] * v + f.ctm[8] * f.eyen;
+        float tin, tout;
+        if (ray_box(f.gdconst, f.origx, f.origy, f.origz, dx, dy, dz, tin, tout)) {
+            float t0 = tin > 0.0f ? tin : 0.0f;
+            float len = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+            float dt = f.step / len;
+            bool done = false;
+            for (int s = 0; s < f.nb && !done; s++) {
+                const int k = f.order[s];
+                if (f.single >= 0 && k != f.single) continue;
+                const DevBrick &b = f.b[k];
+                if (!in_rect(b, i, j)) continue;
+                if (SKIP && b.empty != nullptr)
+                    march_cfg<DT, true>(f, b, dx, dy, dz, t0, dt, acc, done, nexec);
+                else
+                    march_cfg<DT, false>(f, b, dx, dy, dz, t0, dt, acc, done, nexec);
+            }
+        }
+    }
+    const long long o = (long long) oi * f.out_w + oj;
+    if (out32) out32[o] = acc;
+    if (out8) out8[o] = make_uchar4(q8(acc.x), q8(acc.y), q8(acc.z), q8(acc.w));
+    count_exec(f, nexec);
+}
+
+template <int DT>
+cudaError_t launch_dt(const FrameDesc &f, float4 *o32, uchar4 *o8, cudaStream_t s)
+{
+    dim3 grid((f.out_w + kBlockX - 1) / kBlockX, (f.out_h + kBlockY - 1) / kBlockY);
+    if (f.preset == IVR_PRESET_CONFIG) {
+        bool skip = false;
+        for (int k = 0; k < f.nb; k++) skip |= f.b[k].empty != nullptr;
+        if (skip) march_cfg_kernel<DT, true><<<grid, kThreads, 0, s>>>(f, o32, o8);
+        else march_cfg_kernel<DT, false><<<grid, kThreads, 0, s>>>(f, o32, o8);
+        return cudaGetLastError();
+    }
+    switch (f.tf_mode) {
+    case IVR_TF_SEISMIC: march_ref_kernel<DT, IVR_TF_SEISMIC><<<grid, kThreads, 0, s>>>(f, o32, o8); break;
+    case IVR_TF_MED: march_ref_kernel<DT, IVR_TF_MED><<<grid, kThreads, 0, s>>>(f, o32, o8); break;
+    case IVR_TF_SEISMIC2: march_ref_kernel<DT, IVR_TF_SEISMIC2><<<grid, kThreads, 0, s>>>(f, o32, o8); break;
+    case IVR_TF_CHEM: march_ref_kernel<DT, IVR_TF_CHEM><<<grid, kThreads, 0, s>>>(f, o32, o8); break;
+    case IVR_TF_BLEND: march_ref_kernel<DT, IVR_TF_BLEND><<<grid, kThreads, 0, s>>>(f, o32, o8); break;
+    case IVR_TF_RGBBLEND: march_ref_kernel<DT, IVR_TF_RGBBLEND><<<grid, kThreads, 0, s>>>(f, o32, o8); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s)
+{
+    if (f.out_w <= 0 || f.out_h <= 0) return cudaSuccess;
+    switch (f.dtype) {
+    case IVR_U8: return launch_dt<IVR_U8>(f, out32, out8, s);
+    case IVR_U16: return launch_dt<IVR_U16>(f, out32, out8, s);
+    case IVR_F32: return launch_dt<IVR_F32>(f, out32, out8, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace ivr

@@ -1,0 +1,46 @@
+"""CPU: the C-ABI library loads and exports every function include/ivr_gpu.h
+declares, with the declared record sizes (no device calls)."""
+import ctypes
+import os
+import re
+
+from conftest import ROOT
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "ivr_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_ \*]*?\b(ivr_[a-z0-9_]+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ["ivr_create", "ivr_volume_load", "ivr_bricks_setup", "ivr_set_view", "ivr_tf_set_colormap",
+                 "ivr_render", "ivr_render_tile", "ivr_render_brick", "ivr_composite", "ivr_quantize"]:
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    missing = [n for n in declared_functions() if not hasattr(gpu_lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(gpu_lib):
+    from ivr_gb300 import _lib
+    assert set(declared_functions()) <= set(_lib.SIGNATURES)
+
+
+def test_record_sizes():
+    from ivr_gb300._lib import FrameInfo, RenderParams
+    from ivr_gb300.state import IvrState
+    assert ctypes.sizeof(IvrState) == 184
+    assert ctypes.sizeof(RenderParams) == 32
+    assert ctypes.sizeof(FrameInfo) == 12 + 64 * 4 + 64 * 24 + 64 * 16
+
+
+def test_errors_without_device(gpu_lib):
+    # argument checks that return before any CUDA call
+    assert gpu_lib.ivr_destroy(None) == -1
+    assert gpu_lib.ivr_create(0, 0, None) == -1
+    assert gpu_lib.ivr_last_error(None) == b"null context"

@@ -1,0 +1,282 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's golden
+frames and the O2 oracle.
+
+REF preset: bitwise against the reference (composited RGBA32 frames,
+per-brick sub-images, LUTs), RGBA8 exactly the reference's rounding rule.
+CONFIG preset: bitwise against O2 with the same knobs; the tolerance the
+comparison would accept otherwise (max |d| <= 1/255 on RGBA8, 1e-4 relative
+on RGBA32) is what the benchmark claims.
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_case
+from ivr_gb300 import api, synth
+from ivr_gb300.state import orbit_state
+
+pytestmark = pytest.mark.gpu
+
+RGBA8_TOL = 1  # 1/255 per channel
+RGBA32_RTOL = 1e-4
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def dev_frame(vh, vw):
+    import torch
+    return (torch.full((vh, vw, 4), -7.0, dtype=torch.float32, device="cuda"),
+            torch.full((vh, vw, 4), 7, dtype=torch.uint8, device="cuda"))
+
+
+def host(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def load_case_volume(ctx, c):
+    vol = c["volume"]
+    if bool(c["big_endian"]):
+        raw = np.ascontiguousarray(vol.astype(">f4")).view(np.float32)
+        return ctx.load_volume(raw, byteswap=True)
+    return ctx.load_volume(vol)
+
+
+def case_tf(ctx, v, c):
+    tf = ctx.transfer_function()
+    if c["colormap"] == -1:
+        tf.set_lut(c["lut"], c["lutoffset"], 1.0, c["xfer"])
+    else:
+        tf.set_colormap(v, c["colormap"], c["xfer"])
+    return tf
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: p.split("/")[-1][:-4])
+def test_ref_preset_matches_reference_golden(ctx, oracle_mod, path):
+    c = load_case(path)
+    v = load_case_volume(ctx, c)
+    try:
+        if np.prod(c["procdims"]) > 1:
+            v.bricks(*c["procdims"], overlap=1)
+        tf = case_tf(ctx, v, c)
+        lut, off = tf.get_lut()
+        assert off == c["lutoffset"] and np.array_equal(bits(lut), bits(c["lut"]))
+        view = ctx.view().set(v, c["state_obj"], api.ref_params(tile=c["tile"]))
+        vh, vw = c["rgba32"].shape[:2]
+        info = view.info()
+        assert (info["vw"], info["vh"]) == (vw, vh)
+        K = int(np.prod(c["procdims"]))
+        ref_order = [int(k) for k in np.argsort(c["info"][:K, 6], kind="stable")]
+        assert info["order"] == ref_order
+        o32, o8 = dev_frame(vh, vw)
+        view.render(tf, o32.data_ptr(), o8.data_ptr())
+        got32, got8 = host(o32), host(o8)
+        assert np.array_equal(bits(got32), bits(c["rgba32"])), \
+            f"max |d| {np.abs(got32 - c['rgba32']).max()}"
+        assert np.array_equal(got8, oracle_mod.quantize(c["rgba32"]))
+        for k in range(K):
+            b32, _ = dev_frame(vh, vw)
+            view.render_brick(tf, k, b32.data_ptr())
+            assert np.array_equal(bits(host(b32)), bits(c["bricks"][k])), f"brick {k}"
+    finally:
+        v.free()
+
+
+@pytest.mark.parametrize("dtype", ["u16", "f32"])
+def test_ref_preset_dtype_independent(ctx, dtype):
+    c = load_case([p for p in GOLDEN if "8bricks" in p][0])
+    vol = c["volume"].astype(np.uint16 if dtype == "u16" else np.float32)
+    v = ctx.load_volume(vol).bricks(*c["procdims"])
+    tf = case_tf(ctx, v, c)
+    view = ctx.view().set(v, c["state_obj"], api.ref_params(tile=c["tile"]))
+    vh, vw = c["rgba32"].shape[:2]
+    o32, _ = dev_frame(vh, vw)
+    view.render(tf, o32.data_ptr())
+    assert np.array_equal(bits(host(o32)), bits(c["rgba32"]))
+    v.free()
+
+
+def test_volume_file_bigendian(ctx):
+    c = load_case([p for p in GOLDEN if "bigendian" in p][0])
+    d, h, w = c["volume"].shape
+    fd, path = tempfile.mkstemp(suffix=".raw")
+    os.close(fd)
+    try:
+        c["volume"].astype(">f4").tofile(path)
+        v = ctx.load_volume_file(path, w, h, d, api.F32, file_little_endian=False)
+        tf = case_tf(ctx, v, c)
+        view = ctx.view().set(v, c["state_obj"], api.ref_params(tile=c["tile"]))
+        vh, vw = c["rgba32"].shape[:2]
+        o32, _ = dev_frame(vh, vw)
+        view.render(tf, o32.data_ptr())
+        assert np.array_equal(bits(host(o32)), bits(c["rgba32"]))
+        v.free()
+        with pytest.raises(Exception):
+            ctx.load_volume_file(path, w, h, d + 1, api.F32)  # short file
+    finally:
+        os.unlink(path)
+
+
+def test_composite_kernel_matches_reference(ctx):
+    import torch
+    c = load_case([p for p in GOLDEN if "8bricks" in p][0])
+    K = int(np.prod(c["procdims"]))
+    order = [int(k) for k in np.argsort(c["info"][:K, 6], kind="stable")]
+    vh, vw = c["rgba32"].shape[:2]
+    sub = torch.from_numpy(np.ascontiguousarray(c["bricks"][order])).cuda()
+    tile = torch.zeros((vh, vw, 4), dtype=torch.float32, device="cuda")
+    ctx.composite(tile.data_ptr(), sub.data_ptr(), K, vw, vh)
+    assert np.array_equal(bits(host(tile)), bits(c["rgba32"]))
+    out8 = torch.zeros((vh, vw, 4), dtype=torch.uint8, device="cuda")
+    ctx.quantize(tile.data_ptr(), out8.data_ptr(), vh * vw * 4)
+    ctx.composite(tile.data_ptr(), sub.data_ptr(), 0, vw, vh)  # num = 0 is a no-op
+
+
+def test_quantize_boundaries(ctx, oracle_mod):
+    import torch
+    b = ((np.arange(1, 256) - 0.5) / 255).astype(np.float32)
+    x = np.concatenate([b, np.nextafter(b, 0), np.nextafter(b, 1),
+                        np.random.default_rng(1).uniform(-0.1, 1.1, 200000).astype(np.float32),
+                        np.array([0.0, -0.0, 1.0, 1e-38, 1e-45, np.inf, -np.inf, np.nan], np.float32)])
+    # every float within 2^12 ulps of each rounding boundary
+    ub = b.view(np.uint32).astype(np.int64)
+    near = (ub[:, None] + np.arange(-4096, 4097)[None, :]).reshape(-1).astype(np.uint32).view(np.float32)
+    x = np.concatenate([x, near]).astype(np.float32)
+    src = torch.from_numpy(x).cuda()
+    dst = torch.zeros(len(x), dtype=torch.uint8, device="cuda")
+    ctx.quantize(src.data_ptr(), dst.data_ptr(), len(x))
+    assert np.array_equal(host(dst), oracle_mod.quantize(x))
+
+
+CONFIG_CASES = [
+    # shape, dtype, procdims, az, el, win, step, term, skip
+    ((40, 40, 40), "u8", (1, 1, 1), 30, 20, (64, 64), 0.5, 0.99, False),
+    ((40, 40, 40), "u8", (1, 1, 1), 30, 20, (64, 64), 0.5, 0.99, True),
+    ((36, 44, 40), "f32", (2, 2, 2), 210, -30, (72, 56), 0.5, 0.99, True),
+    ((48, 40, 36), "u16", (2, 2, 2), 100, 45, (64, 48), 0.25, 2.0, True),
+    ((40, 40, 40), "u8", (1, 2, 2), 300, 10, (48, 64), 1.0, 0.99, True),
+]
+
+
+def make_config_volume(shape, dtype, seed):
+    return synth.blob_volume(shape, n_blobs=8, seed=seed, dtype=dtype, zero_fraction=0.5, cell=8)
+
+
+@pytest.mark.parametrize("case", CONFIG_CASES, ids=[str(i) for i in range(len(CONFIG_CASES))])
+def test_config_preset_matches_o2(ctx, oracle_mod, case):
+    shape, dtype, procdims, az, el, win, step, term, skip = case
+    vol = make_config_volume(shape, dtype, 7)
+    lut = synth.ramp_tf(256)
+    scale = 256.0 / 65536.0 if dtype == "u16" else 1.0
+    st = orbit_state(az, el, win[0], win[1], fovy=30.0, alpha=1.0)
+    ref = oracle_mod.render(vol, st, lut, 0, 6, preset=1, procdims=procdims, step=step, term_alpha=term,
+                            lut_scale=scale)
+    v = ctx.load_volume(vol)
+    if np.prod(procdims) > 1:
+        v.bricks(*procdims)
+    tf = ctx.transfer_function().set_lut(lut, 0, scale, api.TF_F2B)
+    p = api.config_params(step=step, term_alpha=term, skip=skip)
+    view = ctx.view().set(v, st, p)
+    o32, o8 = dev_frame(win[1], win[0])
+    view.render(tf, o32.data_ptr(), o8.data_ptr())
+    got32, got8 = host(o32), host(o8)
+    assert np.abs(got8.astype(int) - ref["rgba8"].astype(int)).max() <= RGBA8_TOL
+    assert np.allclose(got32, ref["rgba32"], rtol=RGBA32_RTOL, atol=1e-6)
+    assert np.array_equal(bits(got32), bits(ref["rgba32"])), f"max |d| {np.abs(got32 - ref['rgba32']).max()}"
+    v.free()
+
+
+def test_config_skip_is_lossless_and_cheaper(ctx):
+    vol = make_config_volume((64, 64, 64), "u8", 3)
+    lut = synth.ramp_tf(256)
+    st = orbit_state(45, 30, 96, 96, fovy=30.0, alpha=1.0)
+    v = ctx.load_volume(vol).bricks(2, 2, 2)
+    tf = ctx.transfer_function().set_lut(lut, 0, 1.0, api.TF_F2B)
+    outs, execd = [], []
+    for skip in (False, True):
+        view = ctx.view().set(v, st, api.config_params(skip=skip))
+        o32, _ = dev_frame(96, 96)
+        ctx.samples_executed(reset=True)
+        view.render(tf, o32.data_ptr())
+        outs.append(host(o32))
+        execd.append(ctx.samples_executed())
+    assert np.array_equal(bits(outs[0]), bits(outs[1]))
+    assert execd[1] < execd[0]
+    v.free()
+
+
+def test_tiles_equal_full_frame(ctx):
+    vol = make_config_volume((40, 40, 40), "u8", 9)
+    st = orbit_state(60, -20, 80, 64, fovy=30.0, alpha=1.0)
+    v = ctx.load_volume(vol).bricks(2, 1, 2)
+    tf = ctx.transfer_function().set_lut(synth.ramp_tf(256), 0, 1.0, api.TF_F2B)
+    view = ctx.view().set(v, st, api.config_params())
+    full, full8 = dev_frame(64, 80)
+    view.render(tf, full.data_ptr(), full8.data_ptr())
+    F = host(full)
+    for (x, y, w, h) in [(0, 0, 40, 32), (40, 32, 40, 32), (13, 7, 29, 41)]:
+        t32, t8 = dev_frame(h, w)
+        view.render_tile(tf, x, y, w, h, t32.data_ptr(), t8.data_ptr())
+        assert np.array_equal(bits(host(t32)), bits(F[y:y + h, x:x + w]))
+    with pytest.raises(Exception):
+        view.render_tile(tf, 70, 0, 20, 10, full.data_ptr())
+    v.free()
+
+
+def test_render_host_end_to_end(ctx, oracle_mod):
+    c = load_case(GOLDEN[0])
+    v = load_case_volume(ctx, c)
+    tf = case_tf(ctx, v, c)
+    view = ctx.view()
+    vh, vw = c["rgba32"].shape[:2]
+    out = np.zeros((vh, vw, 4), np.uint8)
+    view.render_host(v, tf, c["state_obj"], api.ref_params(tile=c["tile"]), out)
+    assert np.array_equal(out, oracle_mod.quantize(c["rgba32"]))
+    v.free()
+
+
+def test_minmax_histogram(ctx, oracle_mod):
+    for dtype in ("u8", "u16", "f32"):
+        vol = synth.blob_volume((30, 20, 25), n_blobs=5, seed=2, dtype=dtype)
+        v = ctx.load_volume(vol)
+        mn, mx = v.minmax()
+        assert mn == float(vol.min()) and mx == float(vol.max())
+        hs = int((mx - mn) + 1)
+        if hs <= 70000:
+            h = v.histogram(hs)
+            expect = np.bincount((vol.astype(np.float32) - np.float32(mn)).astype(np.int64).ravel(), minlength=hs)
+            assert np.array_equal(h, expect[:hs])
+        v.free()
+
+
+def test_errors_are_codes_not_crashes(ctx):
+    from ivr_gb300._lib import IvrError
+    with pytest.raises(IvrError):
+        ctx.load_volume(np.zeros((1, 4, 4), np.uint8))
+    v = ctx.load_volume(np.zeros((8, 8, 8), np.uint8))
+    with pytest.raises(IvrError):
+        v.bricks(8, 1, 1)
+    tf = ctx.transfer_function()
+    with pytest.raises(IvrError):
+        ctx.view().render(tf)  # view never set
+    view = ctx.view().set(v, orbit_state(0, 0, 16, 16), api.ref_params())
+    with pytest.raises(IvrError):
+        view.render(tf)  # TF without a LUT
+    tf.set_lut(synth.ramp_tf(256), 0, 1.0, api.TF_F2B)
+    with pytest.raises(IvrError):
+        view.render(tf)  # REF preset with the F2B mode
+    v.free()
+
+
+def test_hbm_budget_admission(ctx):
+    from ivr_gb300._lib import IvrError
+    with api.Context(0, hbm_budget=1 << 20) as small:
+        small.load_volume(np.zeros((32, 32, 32), np.uint8))  # 32 KiB fits
+        with pytest.raises(IvrError) as e:
+            small.load_volume(np.zeros((128, 128, 128), np.uint8))  # 2 MiB does not
+        assert e.value.code == -3
