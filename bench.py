@@ -1,0 +1,364 @@
+#!/usr/bin/env python3
+"""Benchmark of the iVR hot path on one GB300 (one JSON line on stdout).
+
+Default workload (sorted_brick_512): a 512^3 float32 volume of 64 seeded
+Gaussian blobs plus 3-octave value noise (amplitude 0.1), split into 2x2x2
+bricks with a one-voxel halo, rendered at 1024x1024 with sort-last
+compositing of the 8 bricks on device in exact view order, 16^3 macrocell
+empty-space skipping, step 0.5 voxel, front-to-back FP32 accumulation with
+early termination at alpha >= 0.99, 8-bit RGBA output.  A step is one frame
+of a new seeded view (camera at distance 5 in a seeded azimuth/elevation
+direction, 30 degree field of view); the volume stays resident in HBM and is
+larger than L2, so no L2 flush is needed between frames.
+
+value: frames/s with the STATE already on the host side of the launch and
+the RGBA8 frame left in device memory.  e2e: the same frames through
+ivr_render_host (STATE from host memory in, RGBA8 frame copied to pinned
+host memory out, inside the timed region).  Gsamples/s counts the plain
+method's lattice points (no skipping, no termination), so skipping shows
+as a higher rate.
+
+--impl reference times the CPU restatement of the same path (the oracle,
+all host threads) on a bounded sample of the same workload: each step
+renders one band of 1/16 of the image rows, rotating through the frame.
+Under torchrun (N>1) every rank renders its own stream of views (replicas;
+the path has no exchange step), value = all frames / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "sorted_brick_512": dict(shape=(512, 512, 512), dtype="f32", n_blobs=64, noise=0.0, value_noise=0.1,
+                             bricks=(2, 2, 2), image=(1024, 1024), step=0.5, term=0.99, fovy=30.0, seed=2),
+    # same kernel and data type, smaller: the case ncu captures in full
+    "prof_384": dict(shape=(384, 384, 384), dtype="f32", n_blobs=64, noise=0.0, value_noise=0.1,
+                     bricks=(2, 2, 2), image=(512, 512), step=0.5, term=0.99, fovy=30.0, seed=2),
+    "plain_128": dict(shape=(128, 128, 128), dtype="u8", n_blobs=8, noise=0.05, value_noise=0.0,
+                      bricks=(1, 1, 1), image=(512, 512), step=0.5, term=0.99, fovy=30.0, seed=1),
+}
+METRIC = "frames/s & Gsamples/s, learned-skip vs plain GPU at <=1/255 err; p99 ms"
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "march_cfg_sorted_brick_512.txt")
+
+
+def views(seed, n, w, h, fovy):
+    from ivr_gb300.state import orbit_state
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        az, el = float(rng.uniform(0, 360)), float(rng.uniform(-60, 60))
+        out.append(orbit_state(az, el, w, h, fovy=fovy, alpha=1.0))
+    return out
+
+
+def make_volume(wl, device):
+    from ivr_gb300 import synth
+    return synth.blob_volume(wl["shape"], n_blobs=wl["n_blobs"], seed=wl["seed"], dtype=wl["dtype"],
+                             noise=wl["noise"], value_noise=wl["value_noise"], device=device)
+
+
+def lut_scale(wl):
+    return 256.0 / 65536.0 if wl["dtype"] == "u16" else 1.0
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        time.sleep(0.3)
+        self.lines = []
+        if self.p:
+            self.p.terminate()
+            out, _ = self.p.communicate(timeout=10)
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the march kernel from the committed ncu
+    summary (dram__bytes_read.sum + dram__bytes_write.sum), if present."""
+    try:
+        for ln in open(PROFILE_TRAFFIC):
+            if ln.startswith("dram_bytes_per_launch:"):
+                return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(wl, vol, states, budget_s=20.0, threads=0):
+    """The oracle on bands of image rows of the same workload, all threads."""
+    from oracle import oracle
+    from ivr_gb300 import synth
+    lut = synth.ramp_tf(256)
+    w, h = wl["image"]
+    band = h // 16
+    cores = os.cpu_count() or 1
+    prep = oracle.Prepared(vol, wl["bricks"])  # volume load: outside the timing, as for the GPU
+    t0 = time.perf_counter()
+    rows = 0
+    nb = 0
+    while True:
+        b = nb % 16
+        st = states[nb % len(states)]
+        oracle.render(vol, st, lut, 0, 6, preset=1, procdims=wl["bricks"], step=wl["step"], term_alpha=wl["term"],
+                      lut_scale=lut_scale(wl), rows=(b * band, (b + 1) * band), threads=threads or cores,
+                      prepared=prep)
+        rows += band
+        nb += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or nb >= 16:
+            break
+    fps = (rows / h) / el
+    return {"value": fps, "unit": "frames/s", "cores": threads or cores, "kind": "port",
+            "sample": f"{nb} bands of {band} of {h} rows (oracle, CONFIG preset, same volume and views), "
+                      f"{el:.1f} s"}
+
+
+def run_reference(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle
+    from ivr_gb300 import synth
+    vol = make_volume(wl, None if wl["shape"][0] <= 160 else _gen_device())
+    w, h = wl["image"]
+    states = views(wl["seed"] + 100, max(args.steps + args.warmup, 1), w, h, wl["fovy"])
+    lut = synth.ramp_tf(256)
+    band = h // 16
+    cores = os.cpu_count() or 1
+    prep = oracle.Prepared(vol, wl["bricks"])  # volume load: outside the timing
+
+    def step(k):
+        b = k % 16
+        oracle.render(vol, states[k % len(states)], lut, 0, 6, preset=1, procdims=wl["bricks"], step=wl["step"],
+                      term_alpha=wl["term"], lut_scale=lut_scale(wl), rows=(b * band, (b + 1) * band),
+                      threads=cores, prepared=prep)
+
+    for k in range(args.warmup):
+        step(k)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        step(args.warmup + k)
+    el = time.perf_counter() - t0
+    fps = (args.steps / 16.0) / el
+    line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * el / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded blobs; the reference's datasets are not available)",
+            "config": config_of(args, wl),
+            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": f"each step renders 1/16 of the rows ({band} of {h}); value = steps/16 "
+                                       f"frames over the time"},
+            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _gen_device():
+    try:
+        import torch
+        return "cuda" if torch.cuda.is_available() else None
+    except ImportError:
+        return None
+
+
+def config_of(args, wl):
+    w, h = wl["image"]
+    return {"workload": args.workload, "volume": "x".join(map(str, wl["shape"][::-1])) + " " + wl["dtype"],
+            "bricks": "x".join(map(str, wl["bricks"])) + " + 1-voxel halo", "image": f"{w}x{h}",
+            "step_voxels": wl["step"], "early_termination_alpha": wl["term"], "skip": "16^3 macrocell grid",
+            "tf": "256-entry RGBA FP32 ramp", "l2": "inputs larger than L2 (volume resident, > 129 MB)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="sorted_brick_512", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+
+    import torch
+    import torch.distributed as dist
+    from ivr_gb300 import api, synth
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    vol = make_volume(wl, f"cuda:{local}")
+    torch.cuda.empty_cache()  # release the generator's temporaries
+    w, h = wl["image"]
+    nviews = args.steps + args.warmup
+    states = views(wl["seed"] + 100 + 7919 * rank, nviews, w, h, wl["fovy"])
+    lut = synth.ramp_tf(256)
+
+    ctx = api.Context(local)
+    v = ctx.load_volume(vol).bricks(*wl["bricks"], overlap=1)
+    tf = ctx.transfer_function().set_lut(lut, 0, lut_scale(wl), api.TF_F2B)
+    params = api.config_params(step=wl["step"], term_alpha=wl["term"], skip=True)
+    view = ctx.view()
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    o8 = torch.empty((h, w, 4), dtype=torch.uint8, device="cuda")
+
+    # work census of the timed views (diagnostic launches, outside timing)
+    lattice = executed = touched = 0
+    for st in states[args.warmup:]:
+        view.set(v, st, params)
+        c = view.census(tf, sp)
+        lattice += c["lattice"]
+        executed += c["executed"]
+        touched += c["touched_bytes"]
+    torch.cuda.synchronize()
+
+    def frame(k):
+        view.set(v, states[k], params)
+        view.render(tf, None, o8.data_ptr(), sp)
+
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup):
+            frame(k)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            start.record(stream)
+            for k in range(args.steps):
+                ev[k][0].record(stream)
+                frame(args.warmup + k)
+                ev[k][1].record(stream)
+            stop.record(stream)
+            torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        t_ms = start.elapsed_time(stop)
+        kern_ms = [a.elapsed_time(b) for a, b in ev]
+
+        # end to end through ivr_render_host: pinned host output, same views
+        host8 = torch.empty((h, w, 4), dtype=torch.uint8).pin_memory().numpy()
+        for k in range(args.warmup):
+            view.render_host(v, tf, states[k], params, host8, sp)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            view.render_host(v, tf, states[args.warmup + k], params, host8, sp)
+        e2e_s = time.perf_counter() - t0
+
+    t_max = torch.tensor([t_ms, e2e_s * 1000.0], device="cuda")
+    if world > 1:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    t_ms, e2e_ms = float(t_max[0]), float(t_max[1])
+    frames = args.steps * world
+    fps = frames / (t_ms / 1000.0)
+    e2e_fps = frames / (e2e_ms / 1000.0)
+    gsps = lattice * world / (t_ms / 1000.0) / 1e9
+
+    if rank == 0:
+        kavg = statistics.mean(kern_ms)
+        peak, how = peaks()
+        alg_bytes = touched / args.steps + w * h * 4  # compulsory volume bytes + RGBA8 out, per launch
+        achieved = alg_bytes / (kavg / 1000.0) / 1e9
+        traffic = profiled_traffic()
+        line = {
+            "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded blobs + value noise; the reference's datasets are not available)",
+            "config": config_of(args, wl),
+            "gsamples_per_s": gsps,
+            "samples": {"lattice_per_frame": lattice / args.steps, "executed_per_frame": executed / args.steps,
+                        "note": "lattice = plain method without skipping or termination"},
+            "kernel_ms": {"mean": kavg, "p50": statistics.median(kern_ms), "max": max(kern_ms)},
+            "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": 184,
+                    "d2h_bytes_per_step": w * h * 4,
+                    "path": "ivr_render_host: host STATE in, RGBA8 to pinned host memory"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": how,
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "note": "algorithmic bytes = macrocells an executed sample read + RGBA8 output"},
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        if not args.no_cpu_baseline and world == 1:
+            line["cpu_baseline"] = cpu_baseline(wl, vol, states[args.warmup:], budget_s=args.cpu_budget)
+        print(json.dumps(line), flush=True)
+    v.free()
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

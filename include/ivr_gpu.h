@@ -176,6 +176,14 @@ int ivr_render_brick(ivr_view *view, ivr_tf *tf, int brick, float *rgba32_dev, v
 int ivr_render_host(ivr_view *view, ivr_volume *vol, ivr_tf *tf, const ivr_state *state,
                     const ivr_render_params *p, uint8_t *rgba8_host, void *stream);
 
+/* Work census of one CONFIG frame (a diagnostic launch, not for timing):
+ * lattice = sample points of the plain method (every brick, no skipping, no
+ * termination) -- the unit of Gsamples/s; executed = samples actually
+ * taken; touched_bytes = bytes of the macrocells an executed sample read,
+ * the frame's compulsory volume traffic. */
+int ivr_census(ivr_view *view, ivr_tf *tf, unsigned long long *lattice, unsigned long long *executed,
+               unsigned long long *touched_bytes, void *stream);
+
 /* --- compositing and output -------------------------------------------- */
 /* compositetiles (main.c:1203-1218): num sub-images of w*h RGBA floats in
  * near -> far order, composited far -> near onto tilebuf with

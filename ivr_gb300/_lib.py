@@ -76,6 +76,8 @@ SIGNATURES = {
     "ivr_render_tile": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _P]),
     "ivr_render_brick": (_I, [_P, _P, _I, _P, _P]),
     "ivr_render_host": (_I, [_P, _P, _P, ctypes.POINTER(IvrState), ctypes.POINTER(RenderParams), _P, _P]),
+    "ivr_census": (_I, [_P, _P, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong),
+                        ctypes.POINTER(ctypes.c_ulonglong), _P]),
     "ivr_composite": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "ivr_quantize": (_I, [_P, _P, _P, ctypes.c_longlong, _P]),
 }

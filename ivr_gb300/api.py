@@ -202,6 +202,14 @@ class View:
         """createlocalimage(rank): one brick's sub-image over the viewport."""
         self.ctx.check(self.ctx.lib.ivr_render_brick(self.h, tf.h, brick, _vp(rgba32), _vp(stream)))
 
+    def census(self, tf: TransferFunction, stream=None) -> dict:
+        """Plain-method lattice points, executed samples and touched volume
+        bytes of this CONFIG frame (diagnostic launch)."""
+        a, e, t = ctypes.c_ulonglong(), ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        self.ctx.check(self.ctx.lib.ivr_census(self.h, tf.h, ctypes.byref(a), ctypes.byref(e), ctypes.byref(t),
+                                               _vp(stream)))
+        return {"lattice": a.value, "executed": e.value, "touched_bytes": t.value}
+
     def render_host(self, vol: Volume, tf: TransferFunction, state: IvrState, params: RenderParams,
                     out: np.ndarray, stream=None):
         """End to end: STATE in, RGBA8 frame to host memory (out: uint8 [vh, vw, 4])."""

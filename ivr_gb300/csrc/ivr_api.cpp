@@ -7,6 +7,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -179,7 +180,15 @@ int valid_params(ivr_ctx *c, const ivr_render_params *p)
     if (!p) return fail(c, IVR_ERR_INVALID, "null render params");
     if (p->preset != IVR_PRESET_REF && p->preset != IVR_PRESET_CONFIG)
         return fail(c, IVR_ERR_INVALID, "unknown preset %d", p->preset);
-    if (!(p->step > 0.0f)) return fail(c, IVR_ERR_INVALID, "step must be > 0");
+    // bounds that keep every ray's sample count finite and modest
+    if (p->preset == IVR_PRESET_REF) {
+        if (!(p->step >= 1.0e-5f && p->step <= 1.0f)) return fail(c, IVR_ERR_INVALID, "REF step must be in [1e-5, 1]");
+        if (p->max_samples < 1 || p->max_samples > 65536)
+            return fail(c, IVR_ERR_INVALID, "REF max_samples must be in [1, 65536]");
+    } else {
+        if (!(p->step >= 0.01f && p->step <= 64.0f)) return fail(c, IVR_ERR_INVALID, "step must be in [0.01, 64] voxels");
+        if (p->max_samples != 0) return fail(c, IVR_ERR_UNSUPPORTED, "CONFIG samples are not capped");
+    }
     if (p->tilew < 1 || p->tileh < 1) return fail(c, IVR_ERR_INVALID, "tile size must be >= 1");
     return IVR_OK;
 }
@@ -200,7 +209,7 @@ int refresh_empty(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t
 }
 
 int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single, float *o32, uint8_t *o8,
-                  void *stream)
+                  void *stream, std::vector<uint8_t *> *touched = nullptr)
 {
     ivr_ctx *c = view ? view->ctx : nullptr;
     if (!view || !tf) return fail(c, IVR_ERR_INVALID, "null view or transfer function");
@@ -227,6 +236,10 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
         int rc = refresh_empty(view->vol, tf, !(f.alpha != 0.0f), s);
         if (rc) return rc;
         for (int k = 0; k < f.nb; k++) f.b[k].empty = view->vol->bricks[k].empty;
+    }
+    if (touched) {
+        f.census = 1;
+        for (int k = 0; k < f.nb; k++) f.b[k].touched = (*touched)[k];
     }
     CK(c, launch_march(f, (float4 *) o32, (uchar4 *) o8, s));
     return IVR_OK;
@@ -578,6 +591,48 @@ int ivr_render_host(ivr_view *view, ivr_volume *vol, ivr_tf *tf, const ivr_state
     if (rc) return rc;
     CK(c, cudaMemcpyAsync(host8, c->d_frame8, bytes, cudaMemcpyDeviceToHost, (cudaStream_t) stream));
     CK(c, cudaStreamSynchronize((cudaStream_t) stream));
+    return IVR_OK;
+}
+
+int ivr_census(ivr_view *view, ivr_tf *tf, unsigned long long *lattice, unsigned long long *executed,
+               unsigned long long *touched_bytes, void *stream)
+{
+    if (!view) return IVR_ERR_INVALID;
+    ivr_ctx *c = view->ctx;
+    if (!view->valid) return fail(c, IVR_ERR_INVALID, "ivr_set_view has not succeeded on this view");
+    if (view->p.preset != IVR_PRESET_CONFIG) return fail(c, IVR_ERR_UNSUPPORTED, "census needs the CONFIG preset");
+    ivr_volume *vol = view->vol;
+    std::vector<uint8_t *> touched(vol->bricks.size(), nullptr);
+    int rc = IVR_OK;
+    for (size_t k = 0; k < touched.size() && rc == IVR_OK; k++) {
+        rc = dev_alloc(c, mc_cells(vol->bricks[k]), (void **) &touched[k]);
+        if (rc == IVR_OK && cudaMemset(touched[k], 0, mc_cells(vol->bricks[k])) != cudaSuccess) rc = IVR_ERR_CUDA;
+    }
+    unsigned long long cnt[2] = {0, 0};
+    size_t bytes = 0;
+    if (rc == IVR_OK && cudaMemset(c->d_counters, 0, sizeof(unsigned long long) * 4) != cudaSuccess) rc = IVR_ERR_CUDA;
+    if (rc == IVR_OK) rc = render_window(view, tf, 0, 0, view->info.vw, view->info.vh, -1, nullptr, nullptr, stream, &touched);
+    if (rc == IVR_OK && cudaStreamSynchronize((cudaStream_t) stream) != cudaSuccess) rc = IVR_ERR_CUDA;
+    if (rc == IVR_OK && cudaMemcpy(cnt, c->d_counters, sizeof(cnt), cudaMemcpyDeviceToHost) != cudaSuccess) rc = IVR_ERR_CUDA;
+    for (size_t k = 0; k < touched.size() && rc == IVR_OK; k++) {
+        const HostBrick &b = vol->bricks[k];
+        std::vector<uint8_t> h(mc_cells(b));
+        if (cudaMemcpy(h.data(), touched[k], h.size(), cudaMemcpyDeviceToHost) != cudaSuccess) { rc = IVR_ERR_CUDA; break; }
+        for (int cz = 0; cz < b.mcz; cz++)
+            for (int cy = 0; cy < b.mcy; cy++)
+                for (int cx = 0; cx < b.mcx; cx++)
+                    if (h[((size_t) cz * b.mcy + cy) * b.mcx + cx])
+                        bytes += (size_t) std::min(kCell, b.lw - cx * kCell) * std::min(kCell, b.lh - cy * kCell) *
+                                 std::min(kCell, b.ld - cz * kCell) * dtype_size(vol->dtype);
+    }
+    for (size_t k = 0; k < touched.size(); k++)
+        if (touched[k]) dev_free(c, touched[k], mc_cells(vol->bricks[k]));
+    cudaMemset(c->d_counters, 0, sizeof(unsigned long long) * 4);
+    if (rc == IVR_ERR_CUDA) return fail(c, rc, "census launch failed");
+    if (rc) return rc;
+    if (lattice) *lattice = cnt[1];
+    if (executed) *executed = cnt[0];
+    if (touched_bytes) *touched_bytes = bytes;
     return IVR_OK;
 }
 

@@ -25,6 +25,7 @@ struct DevBrick {
     float dir0x, dir0y, dir0z;       // REF: ray direction at (istrt, jstrt)
     const uint8_t *empty;   // per-macrocell "zero opacity" flags, or null
     int mcx, mcy, mcz;      // macrocell grid dims
+    uint8_t *touched;       // census only: cells an executed sample read
 };
 
 // Everything one launch needs, passed by value as a __grid_constant__.
@@ -47,10 +48,16 @@ struct FrameDesc {
     float gdconst[6];        // CONFIG: the clipped global box
     int out_x, out_y, out_w, out_h;  // output window in viewport pixels
     int single;              // >= 0: render only this brick (no compositing)
-    unsigned long long *counters;    // [0] executed samples (nullable)
+    unsigned long long *counters;    // [0] executed samples, [1] lattice
+                                     // points (census) -- nullable
+    int census;              // 1: count lattice points of every brick and
+                             // mark touched cells (diagnostic launch)
     int order[kMaxBricks];   // near -> far
     DevBrick b[kMaxBricks];
 };
+
+// kernel parameters are limited to 32764 bytes
+static_assert(sizeof(FrameDesc) <= 32000, "FrameDesc too large for a kernel parameter");
 
 // Host-side brick record (device array + geometry that does not depend on
 // the view).

@@ -255,13 +255,16 @@ __device__ __forceinline__ bool in_rect(const DevBrick &b, int i, int j)
 
 // CONFIG lattice: t_i = fmaf(i, dt, t0).
 __device__ __forceinline__ float cfg_t(float t0, float dt, int i) { return fmaf((float) i, dt, t0); }
+// First lattice index i >= 0 with t_i >= a.  The estimate is exact up to
+// rounding, so the fix-up loops run a step or two; they are bounded anyway.
+constexpr int kMaxLattice = 1 << 24;
 __device__ __forceinline__ int cfg_first_ge(float t0, float dt, float a)
 {
     if (!(a > t0)) return 0;
     float q = (a - t0) / dt;
-    int i = q > 1.0e9f ? 1000000000 : (int) q;
-    while (i > 0 && cfg_t(t0, dt, i - 1) >= a) i--;
-    while (cfg_t(t0, dt, i) < a) i++;
+    int i = q < (float) kMaxLattice ? (int) q : kMaxLattice;
+    for (int it = 0; it < 64 && i > 0 && cfg_t(t0, dt, i - 1) >= a; it++) i--;
+    for (int it = 0; it < 64 && i < kMaxLattice && cfg_t(t0, dt, i) < a; it++) i++;
     return i;
 }
 
@@ -276,14 +279,18 @@ __device__ __forceinline__ bool cell_empty(const DevBrick &b, int ci, int cj, in
 // cell is transparent are stepped over in one jump: every sample actually
 // taken is computed exactly as without skipping, and a skipped sample would
 // have had zero opacity, which leaves (c, a) unchanged.
-template <int DT, bool SKIP>
+template <int DT, bool SKIP, bool CENSUS>
 __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float dy, float dz, float t0,
-                          float dt, float4 &acc, bool &done, unsigned long long &nexec)
+                          float dt, float4 &acc, bool &done, unsigned long long &nexec, unsigned long long &nlat)
 {
     float tin, tout;
     if (!ray_box(b.dconst, f.origx, f.origy, f.origz, dx, dy, dz, tin, tout)) return;
     int i0 = cfg_first_ge(t0, dt, tin);
     int i1 = cfg_first_ge(t0, dt, tout);
+    if (CENSUS) {
+        nlat += (unsigned long long) max(i1 - i0, 0);
+        if (done) return;
+    }
     const float ox = f.origx, oy = f.origy, oz = f.origz;
     const float opac = f.alpha, term = f.term_alpha;
     for (int i = i0; i < i1; i++) {
@@ -308,13 +315,21 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float
                 float ty = dy > 0.0f ? (hi_y - oy) / dy : (dy < 0.0f ? (lo_y - oy) / dy : FLT_MAX);
                 float tz = dz > 0.0f ? (hi_z - oz) / dz : (dz < 0.0f ? (lo_z - oz) / dz : FLT_MAX);
                 float texit = fminf(tx, fminf(ty, tz));
-                int inext = (int) ((texit - t0) / dt) - 1;
+                float q = (texit - t0) / dt;
+                int inext = (q < (float) kMaxLattice ? (int) q : kMaxLattice) - 1;
                 if (inext > i) i = min(inext, i1) - 1;  // loop ++ lands on inext
                 continue;
             }
         }
         float s = sample_cfg<DT>(b, x, y, z);
         nexec++;
+        if (CENSUS) {
+            float ux = (x - b.bminx) * b.icx, uy = (y - b.bminy) * b.icy, uz = (z - b.bminz) * b.icz;
+            int j = min(max((int) floorf(ux), 0), b.nx - 2) / kCell;
+            int ii = min(max((int) floorf(uy), 0), b.ny - 2) / kCell;
+            int k = min(max((int) floorf(uz), 0), b.nz - 2) / kCell;
+            b.touched[((long long) k * b.mcy + ii) * b.mcx + j] = 1;
+        }
         float4 e = lut_at(f, (int) (s * f.lut_scale) - f.lut_off);
         float al = e.w * opac;
         float wgt = (1.0f - acc.w) * al;
@@ -329,12 +344,20 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float
     }
 }
 
-__device__ __forceinline__ void count_exec(const FrameDesc &f, unsigned long long nexec)
+__device__ __forceinline__ void count_exec(const FrameDesc &f, unsigned long long nexec,
+                                           unsigned long long nlat = 0)
 {
     if (f.counters == nullptr) return;
-    unsigned mask = __activemask();
-    for (int o = 16; o > 0; o >>= 1) nexec += __shfl_xor_sync(mask, nexec, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(f.counters, nexec);
+    // every lane of the warp reaches here (out-of-range pixels store
+    // nothing but still count zero)
+    for (int o = 16; o > 0; o >>= 1) {
+        nexec += __shfl_xor_sync(0xffffffffu, nexec, o);
+        nlat += __shfl_xor_sync(0xffffffffu, nlat, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(f.counters, nexec);
+        if (nlat) atomicAdd(f.counters + 1, nlat);
+    }
 }
 
 __device__ __forceinline__ void pixel_of(const FrameDesc &f, int &i, int &j, int &oi, int &oj)
@@ -352,10 +375,10 @@ __global__ void __launch_bounds__(kThreads) march_ref_kernel(const __grid_consta
 {
     int i, j, oi, oj;
     pixel_of(f, i, j, oi, oj);
-    if (oj >= f.out_w || oi >= f.out_h) return;
+    const bool inside = oj < f.out_w && oi < f.out_h;
     float4 d = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     unsigned long long nexec = 0;
-    if (i < f.vh && j < f.vw) {
+    if (inside && i < f.vh && j < f.vw) {
         // far -> near over of per-brick colours; each brick casts its own ray
         // with the sequential column increments of createlocalimage
         // (main.c:986-999)
@@ -375,23 +398,25 @@ __global__ void __launch_bounds__(kThreads) march_ref_kernel(const __grid_consta
             d = over(cs, d);
         }
     }
-    const long long o = (long long) oi * f.out_w + oj;
-    if (out32) out32[o] = d;
-    if (out8) out8[o] = make_uchar4(q8(d.x), q8(d.y), q8(d.z), q8(d.w));
+    if (inside) {
+        const long long o = (long long) oi * f.out_w + oj;
+        if (out32) out32[o] = d;
+        if (out8) out8[o] = make_uchar4(q8(d.x), q8(d.y), q8(d.z), q8(d.w));
+    }
     count_exec(f, nexec);
 }
 
-template <int DT, bool SKIP>
+template <int DT, bool SKIP, bool CENSUS>
 __global__ void __launch_bounds__(kThreads) march_cfg_kernel(const __grid_constant__ FrameDesc f, float4 *out32,
                                                              uchar4 *out8)
 {
     int i, j, oi, oj;
     pixel_of(f, i, j, oi, oj);
-    if (oj >= f.out_w || oi >= f.out_h) return;
+    const bool inside = oj < f.out_w && oi < f.out_h;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    unsigned long long nexec = 0;
+    unsigned long long nexec = 0, nlat = 0;
     bool any = false;
-    if (i < f.vh && j < f.vw)
+    if (inside && i < f.vh && j < f.vw)
         for (int k = 0; k < f.nb; k++) any |= in_rect(f.b[k], i, j);
     if (any) {
         // ctm * (u, v, 5) at the pixel centre
@@ -405,23 +430,25 @@ __global__ void __launch_bounds__(kThreads) march_cfg_kernel(const __grid_consta
             float t0 = tin > 0.0f ? tin : 0.0f;
             float len = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
             float dt = f.step / len;
-            bool done = false;
-            for (int s = 0; s < f.nb && !done; s++) {
+            bool done = !(dt > 0.0f);
+            for (int s = 0; s < f.nb && (CENSUS || !done); s++) {
                 const int k = f.order[s];
                 if (f.single >= 0 && k != f.single) continue;
                 const DevBrick &b = f.b[k];
                 if (!in_rect(b, i, j)) continue;
                 if (SKIP && b.empty != nullptr)
-                    march_cfg<DT, true>(f, b, dx, dy, dz, t0, dt, acc, done, nexec);
+                    march_cfg<DT, true, CENSUS>(f, b, dx, dy, dz, t0, dt, acc, done, nexec, nlat);
                 else
-                    march_cfg<DT, false>(f, b, dx, dy, dz, t0, dt, acc, done, nexec);
+                    march_cfg<DT, false, CENSUS>(f, b, dx, dy, dz, t0, dt, acc, done, nexec, nlat);
             }
         }
     }
-    const long long o = (long long) oi * f.out_w + oj;
-    if (out32) out32[o] = acc;
-    if (out8) out8[o] = make_uchar4(q8(acc.x), q8(acc.y), q8(acc.z), q8(acc.w));
-    count_exec(f, nexec);
+    if (inside) {
+        const long long o = (long long) oi * f.out_w + oj;
+        if (out32) out32[o] = acc;
+        if (out8) out8[o] = make_uchar4(q8(acc.x), q8(acc.y), q8(acc.z), q8(acc.w));
+    }
+    count_exec(f, nexec, nlat);
 }
 
 template <int DT>
@@ -431,8 +458,13 @@ cudaError_t launch_dt(const FrameDesc &f, float4 *o32, uchar4 *o8, cudaStream_t 
     if (f.preset == IVR_PRESET_CONFIG) {
         bool skip = false;
         for (int k = 0; k < f.nb; k++) skip |= f.b[k].empty != nullptr;
-        if (skip) march_cfg_kernel<DT, true><<<grid, kThreads, 0, s>>>(f, o32, o8);
-        else march_cfg_kernel<DT, false><<<grid, kThreads, 0, s>>>(f, o32, o8);
+        if (f.census) {
+            if (skip) march_cfg_kernel<DT, true, true><<<grid, kThreads, 0, s>>>(f, o32, o8);
+            else march_cfg_kernel<DT, false, true><<<grid, kThreads, 0, s>>>(f, o32, o8);
+        } else {
+            if (skip) march_cfg_kernel<DT, true, false><<<grid, kThreads, 0, s>>>(f, o32, o8);
+            else march_cfg_kernel<DT, false, false><<<grid, kThreads, 0, s>>>(f, o32, o8);
+        }
         return cudaGetLastError();
     }
     switch (f.tf_mode) {

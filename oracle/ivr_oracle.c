@@ -117,6 +117,8 @@ typedef struct {
     v3 dir0;                 /* buildray direction at (istrt, jstrt) */
     v3 invcell;              /* CONFIG: core voxels per world unit */
     float *data;             /* float copy, [ld][lh][lw] */
+    unsigned char *empty;    /* CONFIG skip: transparent macrocells */
+    int mcx, mcy, mcz;
 } brick_t;
 
 static const v3 k_normals[6] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
@@ -488,17 +490,54 @@ static c4 raycast_ref(const orc_scene *sc, const brick_t *b, v3 o, v3 d, const t
  * clipped global box (t0 >= 0); brick k owns the samples with
  * tin_k <= t_i < tout_k.  Front-to-back premultiplied accumulation. */
 static float cfg_t(float t0, float dt, int i) { return fmaf((float) i, dt, t0); }
+#define CFG_MAX_LATTICE (1 << 24)
 static int cfg_first_ge(float t0, float dt, float a)
 {
     if (!(a > t0)) return 0;
     float q = (a - t0) / dt;
-    int i = q > 1.0e9f ? 1000000000 : (int) q;
-    while (i > 0 && cfg_t(t0, dt, i - 1) >= a) i--;
-    while (cfg_t(t0, dt, i) < a) i++;
+    int i = q < (float) CFG_MAX_LATTICE ? (int) q : CFG_MAX_LATTICE;
+    for (int it = 0; it < 64 && i > 0 && cfg_t(t0, dt, i - 1) >= a; it++) i--;
+    for (int it = 0; it < 64 && i < CFG_MAX_LATTICE && cfg_t(t0, dt, i) < a; it++) i++;
     return i;
 }
 
 typedef struct { float r, g, b, a; int done; } acc_t;
+
+#define MC 16
+/* Transparent-cell flags of one brick for a LUT: cell c spans local voxels
+ * [c*16, min(c*16+16, n-1)] per axis; it is transparent when no LUT entry
+ * between (int)(min*scale)-1 and (int)(max*scale)+1 (less the offset) has
+ * non-zero opacity. */
+static void brick_empty(brick_t *b, const orc_scene *sc)
+{
+    b->mcx = (b->lw - 2) / MC + 1;
+    b->mcy = (b->lh - 2) / MC + 1;
+    b->mcz = (b->ld - 2) / MC + 1;
+    b->empty = (unsigned char *) malloc((size_t) b->mcx * b->mcy * b->mcz);
+    int n = sc->lut_n;
+    int *pre = (int *) calloc((size_t) n + 1, sizeof(int));
+    for (int i = 0; i < n; i++) pre[i + 1] = pre[i] + (sc->lut[4 * i + 3] != 0.0f);
+    for (int cz = 0; cz < b->mcz; cz++)
+        for (int cy = 0; cy < b->mcy; cy++)
+            for (int cx = 0; cx < b->mcx; cx++) {
+                float lo = FLT_MAX, hi = -FLT_MAX;
+                int x1 = cx * MC + MC < b->lw - 1 ? cx * MC + MC : b->lw - 1;
+                int y1 = cy * MC + MC < b->lh - 1 ? cy * MC + MC : b->lh - 1;
+                int z1 = cz * MC + MC < b->ld - 1 ? cz * MC + MC : b->ld - 1;
+                for (int z = cz * MC; z <= z1; z++)
+                    for (int y = cy * MC; y <= y1; y++)
+                        for (int x = cx * MC; x <= x1; x++) {
+                            float v = b->data[((size_t) z * b->lh + y) * b->lw + x];
+                            lo = fminf(lo, v);
+                            hi = fmaxf(hi, v);
+                        }
+                int a = clampi((int) (lo * sc->lut_scale) - 1 - sc->lut_offset, 0, n - 1);
+                int c = clampi((int) (hi * sc->lut_scale) + 1 - sc->lut_offset, 0, n - 1);
+                b->empty[((size_t) cz * b->mcy + cy) * b->mcx + cx] =
+                    (sc->state.alpha == 0.0f || pre[c + 1] - pre[a] == 0) ? 1 : 0;
+            }
+    free(pre);
+}
 
 static void march_cfg(const orc_scene *sc, const brick_t *b, v3 o, v3 d, float t0, float dt,
                       const tf_t *tf, acc_t *acc, long long *nalg, long long *nexec)
@@ -512,7 +551,28 @@ static void march_cfg(const orc_scene *sc, const brick_t *b, v3 o, v3 d, float t
     if (acc->done) return;
     for (int i = i0; i < i1; i++) {
         float t = cfg_t(t0, dt, i);
-        float s = sample_cfg(b, fmaf(d.x, t, o.x), fmaf(d.y, t, o.y), fmaf(d.z, t, o.z));
+        float x = fmaf(d.x, t, o.x), y = fmaf(d.y, t, o.y), z = fmaf(d.z, t, o.z);
+        if (b->empty) {
+            float ux = (x - b->bmin.x) * b->invcell.x, uy = (y - b->bmin.y) * b->invcell.y,
+                  uz = (z - b->bmin.z) * b->invcell.z;
+            int cj = clampi((int) floorf(ux), 0, b->lw - 2) / MC;
+            int ci = clampi((int) floorf(uy), 0, b->lh - 2) / MC;
+            int ck = clampi((int) floorf(uz), 0, b->ld - 2) / MC;
+            if (b->empty[((size_t) ck * b->mcy + ci) * b->mcx + cj]) {
+                float lox = b->bmin.x + (float) (cj * MC) / b->invcell.x, hix = b->bmin.x + (float) ((cj + 1) * MC) / b->invcell.x;
+                float loy = b->bmin.y + (float) (ci * MC) / b->invcell.y, hiy = b->bmin.y + (float) ((ci + 1) * MC) / b->invcell.y;
+                float loz = b->bmin.z + (float) (ck * MC) / b->invcell.z, hiz = b->bmin.z + (float) ((ck + 1) * MC) / b->invcell.z;
+                float tx = d.x > 0.0f ? (hix - o.x) / d.x : (d.x < 0.0f ? (lox - o.x) / d.x : FLT_MAX);
+                float ty = d.y > 0.0f ? (hiy - o.y) / d.y : (d.y < 0.0f ? (loy - o.y) / d.y : FLT_MAX);
+                float tz = d.z > 0.0f ? (hiz - o.z) / d.z : (d.z < 0.0f ? (loz - o.z) / d.z : FLT_MAX);
+                float texit = fminf(tx, fminf(ty, tz));
+                float q = (texit - t0) / dt;
+                int inext = (q < (float) CFG_MAX_LATTICE ? (int) q : CFG_MAX_LATTICE) - 1;
+                if (inext > i) i = (inext < i1 ? inext : i1) - 1;
+                continue;
+            }
+        }
+        float s = sample_cfg(b, x, y, z);
         (*nexec)++;
         int idx = (int) (s * sc->lut_scale) - tf->off;
         c4 e = lutat(tf, idx);
@@ -600,8 +660,43 @@ static void over(float *d, const float *s)
     d[3] = s[3] + (1.0f - s[3]) * d[3];
 }
 
+struct orc_prepared {
+    int K;
+    float *data[ORC_MAX_BRICKS];
+};
+
+orc_prepared *orc_prepare(const orc_scene *sc)
+{
+    int K = sc->procdims[0] * sc->procdims[1] * sc->procdims[2];
+    if (K < 1 || K > ORC_MAX_BRICKS) return NULL;
+    orc_prepared *p = (orc_prepared *) calloc(1, sizeof(orc_prepared));
+    view_t v;
+    view_setup(sc, &v);
+    p->K = K;
+    for (int k = 0; k < K; k++) {
+        brick_t b;
+        brick_setup(sc, &v, k, &b);
+        brick_load(sc, &b);
+        p->data[k] = b.data;
+    }
+    return p;
+}
+
+void orc_prepared_free(orc_prepared *p)
+{
+    if (!p) return;
+    for (int k = 0; k < p->K; k++) free(p->data[k]);
+    free(p);
+}
+
 int orc_render(const orc_scene *sc, int nthreads, float *rgba32, unsigned char *rgba8,
                float *bricks, orc_stats *st)
+{
+    return orc_render_prepared(sc, NULL, nthreads, rgba32, rgba8, bricks, st);
+}
+
+int orc_render_prepared(const orc_scene *sc, const orc_prepared *prep, int nthreads, float *rgba32,
+                        unsigned char *rgba8, float *bricks, orc_stats *st)
 {
     int K = sc->procdims[0] * sc->procdims[1] * sc->procdims[2];
     if (K < 1 || K > ORC_MAX_BRICKS) return -1;
@@ -615,9 +710,12 @@ int orc_render(const orc_scene *sc, int nthreads, float *rgba32, unsigned char *
     int vw = v.vw, vh = v.vh;
     if (vw < 1 || vh < 1) return -4;
     brick_t *bs = (brick_t *) calloc((size_t) K, sizeof(brick_t));
+    if (prep && prep->K != K) { free(bs); return -5; }
     for (int k = 0; k < K; k++) {
         brick_setup(sc, &v, k, &bs[k]);
-        brick_load(sc, &bs[k]);
+        if (prep) bs[k].data = prep->data[k];
+        else brick_load(sc, &bs[k]);
+        if (sc->skip && sc->preset == ORC_PRESET_CONFIG) brick_empty(&bs[k], sc);
     }
     int order[ORC_MAX_BRICKS];
     if (sc->order == ORC_ORDER_AXIS) {
@@ -688,7 +786,7 @@ int orc_render(const orc_scene *sc, int nthreads, float *rgba32, unsigned char *
                 float t0 = tin > 0.0f ? tin : 0.0f;
                 float len = sqrtf(fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)));
                 float dt = step_world / len;
-                acc_t acc = {0.0f, 0.0f, 0.0f, 0.0f, 0};
+                acc_t acc = {0.0f, 0.0f, 0.0f, 0.0f, !(dt > 0.0f)};
                 size_t p = ((size_t) i * vw + j) * 4;
                 for (int s = 0; s < K; s++) {
                     const brick_t *b = &bs[order[s]];
@@ -721,7 +819,10 @@ int orc_render(const orc_scene *sc, int nthreads, float *rgba32, unsigned char *
         }
     }
     free(img);
-    for (int k = 0; k < K; k++) free(bs[k].data);
+    for (int k = 0; k < K; k++) {
+        if (!prep) free(bs[k].data);
+        free(bs[k].empty);
+    }
     free(bs);
     return K;
 }

@@ -60,6 +60,8 @@ typedef struct {
     float term_alpha;      /* CONFIG: stop at A >= term_alpha (> 1 = never) */
     int order;             /* ORC_ORDER_* */
     int row0, row1;        /* render rows [row0,row1); row1 <= 0 = all */
+    int skip;              /* CONFIG: step over 16^3 macrocells whose samples
+                              all have zero opacity (must not change output) */
 } orc_scene;
 
 typedef struct {
@@ -76,6 +78,15 @@ typedef struct {
  * Returns the brick count, or a negative error. */
 int orc_render(const orc_scene *sc, int nthreads, float *rgba32,
                unsigned char *rgba8, float *bricks, orc_stats *st);
+
+/* Brick arrays of a scene's volume, extracted once (the reference reads
+ * its brick at start-up, main.c:316); orc_render_prepared reuses them for
+ * any view of the same volume and brick grid. */
+typedef struct orc_prepared orc_prepared;
+orc_prepared *orc_prepare(const orc_scene *sc);
+void orc_prepared_free(orc_prepared *p);
+int orc_render_prepared(const orc_scene *sc, const orc_prepared *p, int nthreads, float *rgba32,
+                        unsigned char *rgba8, float *bricks, orc_stats *st);
 
 /* Premultiplied over, far -> near, in the given near->far order
  * (compositetiles, main.c:1203-1218). */

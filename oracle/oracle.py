@@ -34,7 +34,7 @@ class OrcScene(ctypes.Structure):
                 ("lut", ctypes.POINTER(ctypes.c_float)), ("lut_n", ctypes.c_int), ("lut_offset", ctypes.c_int),
                 ("lut_scale", ctypes.c_float), ("tf_mode", ctypes.c_int), ("preset", ctypes.c_int),
                 ("step", ctypes.c_float), ("max_samples", ctypes.c_int), ("term_alpha", ctypes.c_float),
-                ("order", ctypes.c_int), ("row0", ctypes.c_int), ("row1", ctypes.c_int)]
+                ("order", ctypes.c_int), ("row0", ctypes.c_int), ("row1", ctypes.c_int), ("skip", ctypes.c_int)]
 
 
 class OrcStats(ctypes.Structure):
@@ -82,6 +82,12 @@ def o2():
         lib.orc_render.restype = ctypes.c_int
         lib.orc_render.argtypes = [ctypes.POINTER(OrcScene), ctypes.c_int, _FP, ctypes.c_void_p, _FP,
                                    ctypes.POINTER(OrcStats)]
+        lib.orc_prepare.restype = ctypes.c_void_p
+        lib.orc_prepare.argtypes = [ctypes.POINTER(OrcScene)]
+        lib.orc_prepared_free.argtypes = [ctypes.c_void_p]
+        lib.orc_render_prepared.restype = ctypes.c_int
+        lib.orc_render_prepared.argtypes = [ctypes.POINTER(OrcScene), ctypes.c_void_p, ctypes.c_int, _FP,
+                                            ctypes.c_void_p, _FP, ctypes.POINTER(OrcStats)]
         lib.orc_composite.argtypes = [_FP, _FP, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int]
         lib.orc_quantize.argtypes = [_FP, ctypes.c_void_p, ctypes.c_longlong]
         lib.orc_colormap.argtypes = [ctypes.c_int, _FP, ctypes.c_int, ctypes.c_float, ctypes.c_float]
@@ -115,10 +121,53 @@ def viewport(state: IvrState, tile) -> tuple:
     return (state.winwidth // tile[0]) * tile[0], (state.winheight // tile[1]) * tile[1]
 
 
+class Prepared:
+    """Brick arrays of one volume and brick grid, extracted once."""
+
+    def __init__(self, vol: np.ndarray, procdims=(1, 1, 1)):
+        self.vol = np.ascontiguousarray(vol)
+        self.procdims = tuple(procdims)
+        sc = _scene(self.vol, None, None, 0, 0, procdims, (1, 1))
+        self.h = o2().orc_prepare(ctypes.byref(sc))
+        if not self.h:
+            raise RuntimeError("orc_prepare failed")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            o2().orc_prepared_free(self.h)
+            self.h = None
+
+
+def _scene(vol, state, lut_arr, lut_offset, tf_mode, procdims, tile):
+    d, h, w = vol.shape
+    sc = OrcScene()
+    sc.data = vol.ctypes.data
+    sc.dtype = DT_CODE[vol.dtype]
+    sc.gw, sc.gh, sc.gd = w, h, d
+    for i in range(3):
+        sc.procdims[i] = procdims[i]
+    sc.overlap = 1
+    if state is not None:
+        sc.state = state
+    else:
+        sc.state.winwidth = sc.state.winheight = 1
+    sc.tilew, sc.tileh = tile
+    if lut_arr is not None:
+        sc.lut = lut_arr.ctypes.data_as(_FP)
+        sc.lut_n = len(lut_arr)
+    sc.lut_offset = lut_offset
+    sc.tf_mode = tf_mode
+    return sc
+
+
 def render(vol: np.ndarray, state: IvrState, lut: np.ndarray, lut_offset: int, tf_mode: int, *,
            procdims=(1, 1, 1), tile=(1, 1), preset=PRESET_REF, step=None, max_samples=None, term_alpha=None,
-           order=None, lut_scale=1.0, rows=None, threads=0, bricks=False):
+           order=None, lut_scale=1.0, rows=None, threads=0, bricks=False, prepared: "Prepared" = None,
+           skip=False):
     """O2 frame.  Returns dict(rgba32, rgba8, bricks, stats)."""
+    if prepared is not None:
+        vol = prepared.vol
+        assert tuple(procdims) == prepared.procdims
     vol = np.ascontiguousarray(vol)
     d, h, w = vol.shape
     sc = OrcScene()
@@ -143,13 +192,15 @@ def render(vol: np.ndarray, state: IvrState, lut: np.ndarray, lut_offset: int, t
     sc.term_alpha = term_alpha if term_alpha is not None else (2.0 if ref else 0.99)
     sc.order = order if order is not None else (ORDER_CENTER if ref else ORDER_AXIS)
     sc.row0, sc.row1 = rows if rows is not None else (0, 0)
+    sc.skip = int(skip)
     vw, vh = viewport(state, tile)
     K = procdims[0] * procdims[1] * procdims[2]
     rgba32 = np.zeros((vh, vw, 4), np.float32)
     rgba8 = np.zeros((vh, vw, 4), np.uint8)
     bimg = np.zeros((K, vh, vw, 4), np.float32) if bricks else None
     st = OrcStats()
-    rc = o2().orc_render(ctypes.byref(sc), threads, _fp(rgba32), rgba8.ctypes.data, _fp(bimg), ctypes.byref(st))
+    rc = o2().orc_render_prepared(ctypes.byref(sc), prepared.h if prepared is not None else None, threads,
+                                  _fp(rgba32), rgba8.ctypes.data, _fp(bimg), ctypes.byref(st))
     if rc != K:
         raise RuntimeError(f"orc_render failed: {rc}")
     stats = {"samples_alg": st.samples_alg, "samples_exec": st.samples_exec, "order": list(st.order[:K]),

@@ -207,6 +207,11 @@ def test_config_skip_is_lossless_and_cheaper(ctx):
         execd.append(ctx.samples_executed())
     assert np.array_equal(bits(outs[0]), bits(outs[1]))
     assert execd[1] < execd[0]
+    # the oracle's model of the same skipping takes exactly as many samples
+    from oracle import oracle
+    ref = oracle.render(vol, st, lut, 0, 6, preset=1, procdims=(2, 2, 2), skip=True)
+    assert np.array_equal(bits(outs[1]), bits(ref["rgba32"]))
+    assert ref["stats"]["samples_exec"] == execd[1]
     v.free()
 
 

@@ -138,3 +138,14 @@ def test_config_early_termination_bound(oracle_mod):
     b = oracle_mod.render(vol, st, lut, 0, 6, preset=1, term_alpha=2.0)
     assert a["stats"]["samples_exec"] <= b["stats"]["samples_exec"]
     assert np.abs(a["rgba32"] - b["rgba32"]).max() <= 0.0101
+
+
+@pytest.mark.parametrize("procdims", [(1, 1, 1), (2, 2, 2), (1, 3, 2)])
+def test_config_skip_lossless_in_oracle(oracle_mod, procdims):
+    vol = synth.blob_volume((48, 48, 48), n_blobs=8, seed=1, dtype="u8", zero_fraction=0.5, cell=8)
+    st = orbit_state(35, 20, 64, 64, fovy=30.0, alpha=1.0)
+    lut = synth.ramp_tf(256)
+    a = oracle_mod.render(vol, st, lut, 0, 6, preset=1, procdims=procdims)
+    b = oracle_mod.render(vol, st, lut, 0, 6, preset=1, procdims=procdims, skip=True)
+    assert np.array_equal(bits(a["rgba32"]), bits(b["rgba32"]))
+    assert b["stats"]["samples_exec"] < a["stats"]["samples_exec"]
