@@ -30,7 +30,9 @@
  * message of the last failure on a context.  Buffers named *_dev are device
  * pointers; device work is queued on the caller's stream (a cudaStream_t
  * passed as void*, NULL = the legacy default stream).  Handles are not
- * thread-safe: use one context per host thread, or serialise calls.
+ * thread-safe: use one context per host thread, or serialise calls.  A view
+ * owns the work counter of its launches: launches of one view must be
+ * ordered (one stream); use one view per stream for concurrent frames.
  * Images are [h][w] rows of RGBA, row 0 at the bottom (GL raster order).
  */
 #ifndef IVR_GPU_H
@@ -120,9 +122,6 @@ int ivr_create(int device, size_t hbm_budget_bytes, ivr_ctx **out); /* budget 0 
 int ivr_destroy(ivr_ctx *ctx);
 const char *ivr_last_error(const ivr_ctx *ctx);
 int ivr_mem_used(const ivr_ctx *ctx, size_t *bytes);
-/* Samples the march kernels executed since the last reset (a diagnostic
- * counter: skipped and terminated samples are not counted). */
-int ivr_counters(ivr_ctx *ctx, unsigned long long *samples_exec, int reset);
 
 /* --- volume load / brick setup (readvoldata, readfromfile, initvolbbox) -- */
 /* Copies a host volume (x fastest, [d][h][w]) to the device.  byteswap != 0

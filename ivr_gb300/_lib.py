@@ -56,7 +56,6 @@ SIGNATURES = {
     "ivr_destroy": (_I, [_P]),
     "ivr_last_error": (ctypes.c_char_p, [_P]),
     "ivr_mem_used": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
-    "ivr_counters": (_I, [_P, ctypes.POINTER(ctypes.c_ulonglong), _I]),
     "ivr_volume_load": (_I, [_P, _P, _I, _I, _I, _I, _I, ctypes.POINTER(_P)]),
     "ivr_volume_load_file": (_I, [_P, ctypes.c_char_p, _I, _I, _I, _I, _I, ctypes.POINTER(_P)]),
     "ivr_volume_free": (_I, [_P]),

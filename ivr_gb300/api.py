@@ -80,11 +80,6 @@ class Context:
         self.check(self.lib.ivr_mem_used(self.h, ctypes.byref(v)))
         return v.value
 
-    def samples_executed(self, reset: bool = False) -> int:
-        v = ctypes.c_ulonglong()
-        self.check(self.lib.ivr_counters(self.h, ctypes.byref(v), int(reset)))
-        return v.value
-
     def load_volume(self, vol: np.ndarray, byteswap: bool = False) -> "Volume":
         """readvoldata: a (d, h, w) uint8/uint16/float32 array to the device."""
         vol = np.ascontiguousarray(vol)

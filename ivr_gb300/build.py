@@ -40,14 +40,17 @@ def _run(cmd, log):
 
 
 def build(verbose: bool = False) -> str:
+    """Compiles every source and links the library; IVR_NVCC_EXTRA adds
+    nvcc flags (for tuning builds)."""
     os.makedirs(BUILD, exist_ok=True)
+    extra = os.environ.get("IVR_NVCC_EXTRA", "").split()
     cu, cpp = sources()
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
     jobs, objs = [], []
     for f in cu:
         o = os.path.join(BUILD, f + ".o")
         objs.append(o)
-        jobs.append([NVCC, *ARCH, *CU_FLAGS, *inc, "-c", os.path.join(CSRC, f), "-o", o])
+        jobs.append([NVCC, *ARCH, *CU_FLAGS, *extra, *inc, "-c", os.path.join(CSRC, f), "-o", o])
     for f in cpp:
         o = os.path.join(BUILD, f + ".o")
         objs.append(o)

@@ -52,6 +52,9 @@ struct ivr_tf {
 struct ivr_view {
     ivr_ctx *ctx = nullptr;
     ivr_volume *vol = nullptr;
+    unsigned long long *d_tickets = nullptr;  // tile tickets of CONFIG launches
+    unsigned long long ticket_base = 0;
+    bool tickets_dirty = true;
     ivr_render_params p{};
     ivr_state st{};
     bool valid = false;
@@ -230,7 +233,7 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
     f.lut_scale = tf->scale;
     f.out_x = x; f.out_y = y; f.out_w = w; f.out_h = h;
     f.single = single;
-    f.counters = c->d_counters;
+    f.counters = touched ? c->d_counters : nullptr;  // census launches count
     const bool skip = view->p.skip == IVR_SKIP_GRID && view->p.preset == IVR_PRESET_CONFIG;
     if (skip) {
         int rc = refresh_empty(view->vol, tf, !(f.alpha != 0.0f), s);
@@ -241,7 +244,20 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
         f.census = 1;
         for (int k = 0; k < f.nb; k++) f.b[k].touched = (*touched)[k];
     }
-    CK(c, launch_march(f, (float4 *) o32, (uchar4 *) o8, s));
+    if (view->tickets_dirty) {
+        CK(c, cudaMemsetAsync(view->d_tickets, 0, sizeof(unsigned long long), s));
+        view->ticket_base = 0;
+        view->tickets_dirty = false;
+    }
+    f.tickets = view->d_tickets;
+    f.ticket_base = view->ticket_base;
+    long long used = 0;
+    cudaError_t e = launch_march(f, (float4 *) o32, (uchar4 *) o8, s, &used);
+    if (e != cudaSuccess) {
+        view->tickets_dirty = true;
+        return cuda_fail(c, e, "march launch");
+    }
+    view->ticket_base += (unsigned long long) used;
     return IVR_OK;
 }
 
@@ -318,14 +334,6 @@ int ivr_mem_used(const ivr_ctx *c, size_t *bytes)
     return IVR_OK;
 }
 
-int ivr_counters(ivr_ctx *c, unsigned long long *samples_exec, int reset)
-{
-    if (!c) return IVR_ERR_INVALID;
-    if (samples_exec) CK(c, cudaMemcpy(samples_exec, c->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-    if (reset) CK(c, cudaMemset(c->d_counters, 0, sizeof(unsigned long long) * 4));
-    return IVR_OK;
-}
-
 int ivr_volume_load(ivr_ctx *c, const void *host, int w, int h, int d, int dtype, int byteswap, ivr_volume **out)
 {
     if (!c || !out) return IVR_ERR_INVALID;
@@ -333,7 +341,8 @@ int ivr_volume_load(ivr_ctx *c, const void *host, int w, int h, int d, int dtype
     if (!host) return fail(c, IVR_ERR_INVALID, "null volume data");
     if (w < 2 || h < 2 || d < 2) return fail(c, IVR_ERR_INVALID, "volume %dx%dx%d: every dimension must be >= 2", w, h, d);
     if (dtype != IVR_U8 && dtype != IVR_U16 && dtype != IVR_F32) return fail(c, IVR_ERR_INVALID, "dtype %d", dtype);
-    if ((long long) w * h * d >= (1LL << 40)) return fail(c, IVR_ERR_UNSUPPORTED, "volume too large");
+    // the kernels index a brick with 32-bit voxel offsets
+    if ((long long) w * h * d >= (1LL << 32)) return fail(c, IVR_ERR_UNSUPPORTED, "volume of 2^32 or more voxels");
     CK(c, cudaSetDevice(c->device));
     ivr_volume *v = new ivr_volume();
     v->ctx = c;
@@ -516,6 +525,11 @@ int ivr_view_create(ivr_ctx *c, ivr_view **out)
     if (!c || !out) return IVR_ERR_INVALID;
     ivr_view *v = new ivr_view();
     v->ctx = c;
+    int rc = dev_alloc(c, sizeof(unsigned long long), (void **) &v->d_tickets);
+    if (rc) {
+        delete v;
+        return rc;
+    }
     *out = v;
     return IVR_OK;
 }
@@ -523,6 +537,7 @@ int ivr_view_create(ivr_ctx *c, ivr_view **out)
 int ivr_view_free(ivr_view *v)
 {
     if (!v) return IVR_ERR_INVALID;
+    dev_free(v->ctx, v->d_tickets, sizeof(unsigned long long));
     delete v;
     return IVR_OK;
 }

@@ -193,6 +193,9 @@ int build_frame(int gw, int gh, int gd, int dtype, const HostBrick *bricks, int 
         b.icy = (float) hb.ch / hb.h;
         b.icz = (float) hb.cd / hb.d;
         b.mcx = hb.mcx; b.mcy = hb.mcy; b.mcz = hb.mcz;
+        b.mcwx = (float) kCell / b.icx;
+        b.mcwy = (float) kCell / b.icy;
+        b.mcwz = (float) kCell / b.icz;
         // pzero (main.c:616-618) and setplaneconst (ray.c:44-51)
         float pz0[6] = {hb.bminx * -1.0f, hb.bmaxx * 1.0f, hb.bminy * -1.0f,
                         hb.bmaxy * 1.0f, hb.bminz * -1.0f, hb.bmaxz * 1.0f};

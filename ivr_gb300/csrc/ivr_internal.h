@@ -20,6 +20,7 @@ struct DevBrick {
     float bminx, bminy, bminz;
     float w, h, d;          // aabb.w/h/d
     float icx, icy, icz;    // CONFIG: core voxels per world unit
+    float mcwx, mcwy, mcwz; // CONFIG: world size of one macrocell
     float dconst[6];        // clip-plane constants of this brick
     int istrt, istop, jstrt, jstop;  // pixel rect (createlocalimage)
     float dir0x, dir0y, dir0z;       // REF: ray direction at (istrt, jstrt)
@@ -52,6 +53,8 @@ struct FrameDesc {
                                      // points (census) -- nullable
     int census;              // 1: count lattice points of every brick and
                              // mark touched cells (diagnostic launch)
+    unsigned long long *tickets;     // CONFIG: tile ticket counter (view-owned)
+    unsigned long long ticket_base;  // its value when this launch starts
     int order[kMaxBricks];   // near -> far
     DevBrick b[kMaxBricks];
 };
@@ -93,6 +96,8 @@ cudaError_t launch_quantize(const float *in, uint8_t *out, long long n, cudaStre
 int minmax_parts();
 
 // march (ivr_march.cu)
-cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s);
+// *tickets: how many tile tickets the launch takes from f.tickets (a
+// persistent CONFIG launch takes each tile once and each warp fails once).
+cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s, long long *tickets);
 
 }  // namespace ivr

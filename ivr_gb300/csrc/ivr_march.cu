@@ -17,6 +17,11 @@ namespace {
 constexpr int kBlockX = 16;  // pixels per block: 2x2 warps of 8x4
 constexpr int kBlockY = 8;
 constexpr int kThreads = 128;
+#ifndef IVR_CFG_BLOCKS_PER_SM
+#define IVR_CFG_BLOCKS_PER_SM 8
+#endif
+// resident blocks per SM the CONFIG kernel is compiled for (8 = 64 registers)
+constexpr int kCfgBlocksPerSm = IVR_CFG_BLOCKS_PER_SM;
 
 template <int DT> struct VoxT;
 template <> struct VoxT<IVR_U8> { using T = uint8_t; };
@@ -25,6 +30,12 @@ template <> struct VoxT<IVR_F32> { using T = float; };
 
 template <int DT>
 __device__ __forceinline__ float vload(const void *p, long long i)
+{
+    return (float) __ldg(reinterpret_cast<const typename VoxT<DT>::T *>(p) + i);
+}
+// bricks hold fewer than 2^32 voxels (checked at load), so 32-bit offsets
+template <int DT>
+__device__ __forceinline__ float vload32(const void *p, unsigned i)
 {
     return (float) __ldg(reinterpret_cast<const typename VoxT<DT>::T *>(p) + i);
 }
@@ -121,12 +132,12 @@ __device__ __forceinline__ float sample_cfg(const DevBrick &b, float x, float y,
     float fx = fminf(fmaxf(ux - (float) j, 0.0f), 1.0f);
     float fy = fminf(fmaxf(uy - (float) i, 0.0f), 1.0f);
     float fz = fminf(fmaxf(uz - (float) k, 0.0f), 1.0f);
-    const long long sy = nx, sz = (long long) nx * ny;
-    const long long p = k * sz + i * sy + j;
-    float c00 = lerpf(vload<DT>(b.data, p), vload<DT>(b.data, p + 1), fx);
-    float c10 = lerpf(vload<DT>(b.data, p + sy), vload<DT>(b.data, p + sy + 1), fx);
-    float c01 = lerpf(vload<DT>(b.data, p + sz), vload<DT>(b.data, p + sz + 1), fx);
-    float c11 = lerpf(vload<DT>(b.data, p + sz + sy), vload<DT>(b.data, p + sz + sy + 1), fx);
+    const unsigned sy = (unsigned) nx, sz = (unsigned) nx * (unsigned) ny;
+    const unsigned p = (unsigned) k * sz + (unsigned) i * sy + (unsigned) j;
+    float c00 = lerpf(vload32<DT>(b.data, p), vload32<DT>(b.data, p + 1), fx);
+    float c10 = lerpf(vload32<DT>(b.data, p + sy), vload32<DT>(b.data, p + sy + 1), fx);
+    float c01 = lerpf(vload32<DT>(b.data, p + sz), vload32<DT>(b.data, p + sz + 1), fx);
+    float c11 = lerpf(vload32<DT>(b.data, p + sz + sy), vload32<DT>(b.data, p + sz + sy + 1), fx);
     float c0 = lerpf(c00, c10, fy);
     float c1 = lerpf(c01, c11, fy);
     return lerpf(c0, c1, fz);
@@ -275,64 +286,65 @@ __device__ __forceinline__ bool cell_empty(const DevBrick &b, int ci, int cj, in
 }
 
 // One brick of the CONFIG march: samples tin_k <= t_i < tout_k of the ray's
-// lattice, front-to-back into (c, a).  With a macrocell grid, samples whose
-// cell is transparent are stepped over in one jump: every sample actually
-// taken is computed exactly as without skipping, and a skipped sample would
-// have had zero opacity, which leaves (c, a) unchanged.
+// lattice, front-to-back into acc.  One loop iteration is one lattice index
+// for every lane, so the lanes of a warp stay in step.  With a macrocell grid
+// a lane checks the cell of its sample (by the same index arithmetic the
+// sampler uses) only when it passes the exit of the last opaque cell it
+// checked: a transparent cell's samples are stepped over up to two samples
+// before the ray leaves the cell's box (each skipped sample lies in the cell,
+// so it would have had zero opacity and left acc unchanged); an opaque cell's
+// samples are taken up to one past the exit without further checks.  Every
+// sample that is taken is computed exactly as without skipping.
 template <int DT, bool SKIP, bool CENSUS>
-__device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float dy, float dz, float t0,
-                          float dt, float4 &acc, bool &done, unsigned long long &nexec, unsigned long long &nlat)
+__device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float dy, float dz, float idx,
+                          float idy, float idz, float t0, float dt, float idt, float4 &acc, bool &done,
+                          unsigned long long &nexec, unsigned long long &nlat)
 {
     float tin, tout;
     if (!ray_box(b.dconst, f.origx, f.origy, f.origz, dx, dy, dz, tin, tout)) return;
-    int i0 = cfg_first_ge(t0, dt, tin);
-    int i1 = cfg_first_ge(t0, dt, tout);
+    const int i0 = cfg_first_ge(t0, dt, tin);
+    const int i1 = cfg_first_ge(t0, dt, tout);
     if (CENSUS) {
         nlat += (unsigned long long) max(i1 - i0, 0);
         if (done) return;
     }
     const float ox = f.origx, oy = f.origy, oz = f.origz;
     const float opac = f.alpha, term = f.term_alpha;
+    int icheck = i0;  // next lattice index whose cell must be checked
     for (int i = i0; i < i1; i++) {
-        float t = cfg_t(t0, dt, i);
-        float x = fmaf(dx, t, ox), y = fmaf(dy, t, oy), z = fmaf(dz, t, oz);
-        if (SKIP) {
-            // cell of this sample in the brick's voxel index space
-            float ux = (x - b.bminx) * b.icx, uy = (y - b.bminy) * b.icy, uz = (z - b.bminz) * b.icz;
-            int j = min(max((int) floorf(ux), 0), b.nx - 2);
-            int ii = min(max((int) floorf(uy), 0), b.ny - 2);
-            int k = min(max((int) floorf(uz), 0), b.nz - 2);
-            int cj = j / kCell, ci = ii / kCell, ck = k / kCell;
+        const float t = cfg_t(t0, dt, i);
+        const float x = fmaf(dx, t, ox), y = fmaf(dy, t, oy), z = fmaf(dz, t, oz);
+        if (SKIP && i >= icheck) {
+            const int cj = min(max((int) floorf((x - b.bminx) * b.icx), 0), b.nx - 2) / kCell;
+            const int ci = min(max((int) floorf((y - b.bminy) * b.icy), 0), b.ny - 2) / kCell;
+            const int ck = min(max((int) floorf((z - b.bminz) * b.icz), 0), b.nz - 2) / kCell;
+            // ray parameter where it leaves the cell's box (approximate:
+            // the margins absorb its rounding)
+            const float tx = dx > 0.0f ? (fmaf((float) (cj + 1), b.mcwx, b.bminx) - ox) * idx
+                             : dx < 0.0f ? (fmaf((float) cj, b.mcwx, b.bminx) - ox) * idx : FLT_MAX;
+            const float ty = dy > 0.0f ? (fmaf((float) (ci + 1), b.mcwy, b.bminy) - oy) * idy
+                             : dy < 0.0f ? (fmaf((float) ci, b.mcwy, b.bminy) - oy) * idy : FLT_MAX;
+            const float tz = dz > 0.0f ? (fmaf((float) (ck + 1), b.mcwz, b.bminz) - oz) * idz
+                             : dz < 0.0f ? (fmaf((float) ck, b.mcwz, b.bminz) - oz) * idz : FLT_MAX;
+            const float q = fminf(fmaxf((fminf(tx, fminf(ty, tz)) - t0) * idt, 0.0f), (float) kMaxLattice);
+            const int iexit = (int) q;  // last lattice index at or before the exit
             if (cell_empty(b, ci, cj, ck)) {
-                // exit parameter of this cell's box along the ray, in world
-                // coordinates; jump to one sample before it (the sample there
-                // is re-checked, so rounding in the exit never skips a
-                // non-empty sample)
-                float lo_x = b.bminx + (float) (cj * kCell) / b.icx, hi_x = b.bminx + (float) ((cj + 1) * kCell) / b.icx;
-                float lo_y = b.bminy + (float) (ci * kCell) / b.icy, hi_y = b.bminy + (float) ((ci + 1) * kCell) / b.icy;
-                float lo_z = b.bminz + (float) (ck * kCell) / b.icz, hi_z = b.bminz + (float) ((ck + 1) * kCell) / b.icz;
-                float tx = dx > 0.0f ? (hi_x - ox) / dx : (dx < 0.0f ? (lo_x - ox) / dx : FLT_MAX);
-                float ty = dy > 0.0f ? (hi_y - oy) / dy : (dy < 0.0f ? (lo_y - oy) / dy : FLT_MAX);
-                float tz = dz > 0.0f ? (hi_z - oz) / dz : (dz < 0.0f ? (lo_z - oz) / dz : FLT_MAX);
-                float texit = fminf(tx, fminf(ty, tz));
-                float q = (texit - t0) / dt;
-                int inext = (q < (float) kMaxLattice ? (int) q : kMaxLattice) - 1;
-                if (inext > i) i = min(inext, i1) - 1;  // loop ++ lands on inext
+                i = max(i, iexit - 2);  // the loop's ++ resumes at iexit - 1
                 continue;
             }
+            icheck = iexit + 1;
         }
-        float s = sample_cfg<DT>(b, x, y, z);
-        nexec++;
+        const float s = sample_cfg<DT>(b, x, y, z);
         if (CENSUS) {
-            float ux = (x - b.bminx) * b.icx, uy = (y - b.bminy) * b.icy, uz = (z - b.bminz) * b.icz;
-            int j = min(max((int) floorf(ux), 0), b.nx - 2) / kCell;
-            int ii = min(max((int) floorf(uy), 0), b.ny - 2) / kCell;
-            int k = min(max((int) floorf(uz), 0), b.nz - 2) / kCell;
+            nexec++;
+            int j = min(max((int) floorf((x - b.bminx) * b.icx), 0), b.nx - 2) / kCell;
+            int ii = min(max((int) floorf((y - b.bminy) * b.icy), 0), b.ny - 2) / kCell;
+            int k = min(max((int) floorf((z - b.bminz) * b.icz), 0), b.nz - 2) / kCell;
             b.touched[((long long) k * b.mcy + ii) * b.mcx + j] = 1;
         }
-        float4 e = lut_at(f, (int) (s * f.lut_scale) - f.lut_off);
-        float al = e.w * opac;
-        float wgt = (1.0f - acc.w) * al;
+        const float4 e = lut_at(f, (int) (s * f.lut_scale) - f.lut_off);
+        const float al = e.w * opac;
+        const float wgt = (1.0f - acc.w) * al;
         acc.x = fmaf(wgt, e.x, acc.x);
         acc.y = fmaf(wgt, e.y, acc.y);
         acc.z = fmaf(wgt, e.z, acc.z);
@@ -406,67 +418,126 @@ __global__ void __launch_bounds__(kThreads) march_ref_kernel(const __grid_consta
     count_exec(f, nexec);
 }
 
+// One CONFIG ray: pixel (i, j) of the viewport, all bricks front to back.
 template <int DT, bool SKIP, bool CENSUS>
-__global__ void __launch_bounds__(kThreads) march_cfg_kernel(const __grid_constant__ FrameDesc f, float4 *out32,
-                                                             uchar4 *out8)
+__device__ __forceinline__ float4 ray_cfg(const FrameDesc &f, int i, int j, unsigned long long &nexec,
+                                          unsigned long long &nlat)
 {
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    bool any = false;
+    for (int k = 0; k < f.nb; k++) any |= in_rect(f.b[k], i, j);
+    if (!any) return acc;
+    // ctm * (u, v, 5) at the pixel centre
+    const float u = f.left + ((float) j + 0.5f) * f.du;
+    const float v = f.bottom + ((float) i + 0.5f) * f.dv;
+    const float dx = f.ctm[0] * u + f.ctm[1] * v + f.ctm[2] * f.eyen;
+    const float dy = f.ctm[3] * u + f.ctm[4] * v + f.ctm[5] * f.eyen;
+    const float dz = f.ctm[6] * u + f.ctm[7] * v + f.ctm[8] * f.eyen;
+    float tin, tout;
+    if (!ray_box(f.gdconst, f.origx, f.origy, f.origz, dx, dy, dz, tin, tout)) return acc;
+    const float t0 = tin > 0.0f ? tin : 0.0f;
+    const float len = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+    const float dt = f.step / len;
+    bool done = !(dt > 0.0f);
+    const float idx = 1.0f / dx, idy = 1.0f / dy, idz = 1.0f / dz, idt = 1.0f / dt;
+    for (int s = 0; s < f.nb && (CENSUS || !done); s++) {
+        const int k = f.order[s];
+        if (f.single >= 0 && k != f.single) continue;
+        const DevBrick &b = f.b[k];
+        if (!in_rect(b, i, j)) continue;
+        if (SKIP && b.empty != nullptr)
+            march_cfg<DT, true, CENSUS>(f, b, dx, dy, dz, idx, idy, idz, t0, dt, idt, acc, done, nexec, nlat);
+        else
+            march_cfg<DT, false, CENSUS>(f, b, dx, dy, dz, idx, idy, idz, t0, dt, idt, acc, done, nexec, nlat);
+    }
+    return acc;
+}
+
+// Persistent CONFIG kernel: every warp takes 8x4 pixel tiles from a ticket
+// counter until none are left, so warps that drew short rays pick up more
+// work instead of idling while the grid's last blocks finish.
+#ifndef IVR_CFG_PERSISTENT
+#define IVR_CFG_PERSISTENT 1
+#endif
+
+// One pixel of the output window (ow, oh) = (oj, oi).
+template <int DT, bool SKIP, bool CENSUS>
+__device__ __forceinline__ void pixel_cfg(const FrameDesc &f, int oi, int oj, float4 *out32, uchar4 *out8,
+                                          unsigned long long &nexec, unsigned long long &nlat)
+{
+    if (oj >= f.out_w || oi >= f.out_h) return;
+    const int j = f.out_x + oj, i = f.out_y + oi;
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (i < f.vh && j < f.vw) acc = ray_cfg<DT, SKIP, CENSUS>(f, i, j, nexec, nlat);
+    const long long o = (long long) oi * f.out_w + oj;
+    if (out32) out32[o] = acc;
+    if (out8) out8[o] = make_uchar4(q8(acc.x), q8(acc.y), q8(acc.z), q8(acc.w));
+}
+
+// CONFIG kernel.  Persistent form: every warp takes 8x4 pixel tiles from a
+// ticket counter until none are left, so warps that drew short rays pick up
+// more work instead of idling while the grid's last blocks finish.  Grid
+// form: one thread per pixel, blocks of 2x2 warp tiles.
+template <int DT, bool SKIP, bool CENSUS>
+__global__ void __launch_bounds__(kThreads, kCfgBlocksPerSm) march_cfg_kernel(const __grid_constant__ FrameDesc f,
+                                                                              float4 *out32, uchar4 *out8)
+{
+    unsigned long long nexec = 0, nlat = 0;
+#if IVR_CFG_PERSISTENT
+    const int lane = threadIdx.x & 31;
+    const int tiles_x = (f.out_w + 7) >> 3;
+    const long long ntiles = (long long) tiles_x * ((f.out_h + 3) >> 2);
+    for (;;) {
+        unsigned long long ticket = 0;
+        if (lane == 0) ticket = atomicAdd(f.tickets, 1ull);
+        const long long tile = (long long) (__shfl_sync(0xffffffffu, ticket, 0) - f.ticket_base);
+        if (tile >= ntiles) break;
+        pixel_cfg<DT, SKIP, CENSUS>(f, (int) (tile / tiles_x) * 4 + (lane >> 3), (int) (tile % tiles_x) * 8 + (lane & 7),
+                                    out32, out8, nexec, nlat);
+    }
+#else
     int i, j, oi, oj;
     pixel_of(f, i, j, oi, oj);
-    const bool inside = oj < f.out_w && oi < f.out_h;
-    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    unsigned long long nexec = 0, nlat = 0;
-    bool any = false;
-    if (inside && i < f.vh && j < f.vw)
-        for (int k = 0; k < f.nb; k++) any |= in_rect(f.b[k], i, j);
-    if (any) {
-        // ctm * (u, v, 5) at the pixel centre
-        float u = f.left + ((float) j + 0.5f) * f.du;
-        float v = f.bottom + ((float) i + 0.5f) * f.dv;
-        float dx = f.ctm[0] * u + f.ctm[1] * v + f.ctm[2] * f.eyen;
-        float dy = f.ctm[3] * u + f.ctm[4] * v + f.ctm[5] * f.eyen;
-        float dz = f.ctm[6] * u + f.ctm[7] * v + f.ctm[8] * f.eyen;
-        float tin, tout;
-        if (ray_box(f.gdconst, f.origx, f.origy, f.origz, dx, dy, dz, tin, tout)) {
-            float t0 = tin > 0.0f ? tin : 0.0f;
-            float len = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
-            float dt = f.step / len;
-            bool done = !(dt > 0.0f);
-            for (int s = 0; s < f.nb && (CENSUS || !done); s++) {
-                const int k = f.order[s];
-                if (f.single >= 0 && k != f.single) continue;
-                const DevBrick &b = f.b[k];
-                if (!in_rect(b, i, j)) continue;
-                if (SKIP && b.empty != nullptr)
-                    march_cfg<DT, true, CENSUS>(f, b, dx, dy, dz, t0, dt, acc, done, nexec, nlat);
-                else
-                    march_cfg<DT, false, CENSUS>(f, b, dx, dy, dz, t0, dt, acc, done, nexec, nlat);
-            }
-        }
+    pixel_cfg<DT, SKIP, CENSUS>(f, oi, oj, out32, out8, nexec, nlat);
+#endif
+    if (CENSUS) count_exec(f, nexec, nlat);
+}
+
+template <typename K>
+int persistent_grid(K kernel)
+{
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     }
-    if (inside) {
-        const long long o = (long long) oi * f.out_w + oj;
-        if (out32) out32[o] = acc;
-        if (out8) out8[o] = make_uchar4(q8(acc.x), q8(acc.y), q8(acc.z), q8(acc.w));
-    }
-    count_exec(f, nexec, nlat);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
+    return sms * (per_sm > 0 ? per_sm : 1);
 }
 
 template <int DT>
-cudaError_t launch_dt(const FrameDesc &f, float4 *o32, uchar4 *o8, cudaStream_t s)
+cudaError_t launch_dt(const FrameDesc &f, float4 *o32, uchar4 *o8, cudaStream_t s, long long *warps_launched)
 {
     dim3 grid((f.out_w + kBlockX - 1) / kBlockX, (f.out_h + kBlockY - 1) / kBlockY);
     if (f.preset == IVR_PRESET_CONFIG) {
         bool skip = false;
         for (int k = 0; k < f.nb; k++) skip |= f.b[k].empty != nullptr;
-        if (f.census) {
-            if (skip) march_cfg_kernel<DT, true, true><<<grid, kThreads, 0, s>>>(f, o32, o8);
-            else march_cfg_kernel<DT, false, true><<<grid, kThreads, 0, s>>>(f, o32, o8);
-        } else {
-            if (skip) march_cfg_kernel<DT, true, false><<<grid, kThreads, 0, s>>>(f, o32, o8);
-            else march_cfg_kernel<DT, false, false><<<grid, kThreads, 0, s>>>(f, o32, o8);
-        }
+        auto kern = f.census ? (skip ? march_cfg_kernel<DT, true, true> : march_cfg_kernel<DT, false, true>)
+                             : (skip ? march_cfg_kernel<DT, true, false> : march_cfg_kernel<DT, false, false>);
+#if IVR_CFG_PERSISTENT
+        const int blocks = persistent_grid(kern);
+        // every tile is taken once and every warp ends on one failed take
+        if (warps_launched)
+            *warps_launched = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2) + (long long) blocks * (kThreads / 32);
+        kern<<<blocks, kThreads, 0, s>>>(f, o32, o8);
+#else
+        kern<<<grid, kThreads, 0, s>>>(f, o32, o8);
+#endif
         return cudaGetLastError();
     }
+    if (warps_launched) *warps_launched = 0;
     switch (f.tf_mode) {
     case IVR_TF_SEISMIC: march_ref_kernel<DT, IVR_TF_SEISMIC><<<grid, kThreads, 0, s>>>(f, o32, o8); break;
     case IVR_TF_MED: march_ref_kernel<DT, IVR_TF_MED><<<grid, kThreads, 0, s>>>(f, o32, o8); break;
@@ -481,13 +552,14 @@ cudaError_t launch_dt(const FrameDesc &f, float4 *o32, uchar4 *o8, cudaStream_t 
 
 }  // namespace
 
-cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s)
+cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s, long long *warps)
 {
+    if (warps) *warps = 0;
     if (f.out_w <= 0 || f.out_h <= 0) return cudaSuccess;
     switch (f.dtype) {
-    case IVR_U8: return launch_dt<IVR_U8>(f, out32, out8, s);
-    case IVR_U16: return launch_dt<IVR_U16>(f, out32, out8, s);
-    case IVR_F32: return launch_dt<IVR_F32>(f, out32, out8, s);
+    case IVR_U8: return launch_dt<IVR_U8>(f, out32, out8, s, warps);
+    case IVR_U16: return launch_dt<IVR_U16>(f, out32, out8, s, warps);
+    case IVR_F32: return launch_dt<IVR_F32>(f, out32, out8, s, warps);
     default: return cudaErrorInvalidValue;
     }
 }
