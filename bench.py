@@ -44,7 +44,7 @@ WORKLOADS = {
                              bricks=(2, 2, 2), image=(1024, 1024), step=0.5, term=0.99, fovy=30.0, seed=2),
     # same kernel and data type, smaller: the case ncu captures in full
     "prof_384": dict(shape=(384, 384, 384), dtype="f32", n_blobs=64, noise=0.0, value_noise=0.1,
-                     bricks=(2, 2, 2), image=(512, 512), step=0.5, term=0.99, fovy=30.0, seed=2),
+                     bricks=(2, 2, 2), image=(1024, 1024), step=0.5, term=0.99, fovy=30.0, seed=2),
     "plain_128": dict(shape=(128, 128, 128), dtype="u8", n_blobs=8, noise=0.05, value_noise=0.0,
                       bricks=(1, 1, 1), image=(512, 512), step=0.5, term=0.99, fovy=30.0, seed=1),
 }

@@ -202,8 +202,8 @@ int refresh_empty(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t
 {
     if (v->empty_serial == tf->serial && v->empty_zero_alpha == (int) zero_alpha) return IVR_OK;
     for (auto &b : v->bricks) {
-        if (zero_alpha) CK(v->ctx, cudaMemsetAsync(b.empty, 1, mc_cells(b), s));
-        else CK(v->ctx, launch_empty_flags(b.mc_minmax, (int) mc_cells(b), tf->d_nzprefix, tf->n, tf->off,
+        if (zero_alpha) CK(v->ctx, cudaMemsetAsync(b.empty, kDistCap, mc_cells(b), s));
+        else CK(v->ctx, launch_empty_flags(b.mc_minmax, b.mcx, b.mcy, b.mcz, tf->d_nzprefix, tf->n, tf->off,
                                            tf->scale, b.empty, s));
     }
     v->empty_serial = tf->serial;

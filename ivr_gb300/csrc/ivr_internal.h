@@ -10,6 +10,7 @@ namespace ivr {
 
 constexpr int kMaxBricks = IVR_MAX_BRICKS;
 constexpr int kCell = 16;  // macrocell edge in voxels
+constexpr int kDistCap = 8;  // largest transparent radius stored per macrocell
 
 // One brick as the march kernels see it.  Geometry follows the reference's
 // per-rank AABB (main.c:552-618): bmin and w/h/d from the brick's world
@@ -24,7 +25,9 @@ struct DevBrick {
     float dconst[6];        // clip-plane constants of this brick
     int istrt, istop, jstrt, jstop;  // pixel rect (createlocalimage)
     float dir0x, dir0y, dir0z;       // REF: ray direction at (istrt, jstrt)
-    const uint8_t *empty;   // per-macrocell "zero opacity" flags, or null
+    const uint8_t *empty;   // per macrocell: 0 = some sample there can be
+                            // opaque; r >= 1 = every cell within r-1 cells
+                            // (Chebyshev) is transparent; or null
     int mcx, mcy, mcz;      // macrocell grid dims
     uint8_t *touched;       // census only: cells an executed sample read
 };
@@ -89,8 +92,8 @@ cudaError_t launch_histogram(const void *data, int dtype, long long n, float mn,
                              cudaStream_t s);
 cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int nz, float *mc, int mcx, int mcy,
                               int mcz, cudaStream_t s);
-cudaError_t launch_empty_flags(const float *mc, int ncell, const int *nzprefix, int lut_n, int lut_off,
-                               float lut_scale, uint8_t *empty, cudaStream_t s);
+cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const int *nzprefix, int lut_n,
+                               int lut_off, float lut_scale, uint8_t *empty, cudaStream_t s);
 cudaError_t launch_composite(float *dst, const float *src, int num, long long npix, cudaStream_t s);
 cudaError_t launch_quantize(const float *in, uint8_t *out, long long n, cudaStream_t s);
 int minmax_parts();

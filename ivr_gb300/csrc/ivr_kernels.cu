@@ -139,19 +139,46 @@ __global__ void macrocell_kernel(const void *data, int dtype, int nx, int ny, in
     }
 }
 
-// A cell is empty when no LUT entry its samples can index has non-zero
-// opacity.  Samples lie in [min, max] of the cell's voxels up to rounding,
-// so the index range is widened by one on each side.  nzprefix[i] = number
-// of entries in [0, i) with non-zero opacity.
+// A cell is transparent when no LUT entry its samples can index has
+// non-zero opacity.  Samples lie in [min, max] of the cell's voxels up to
+// rounding, so the index range is widened by one on each side.
+// nzprefix[i] = number of entries in [0, i) with non-zero opacity.
+// Writes kDistCap for a transparent cell and 0 for the others.
 __global__ void empty_kernel(const float *mc, int ncell, const int *nzprefix, int lut_n, int lut_off,
-                             float lut_scale, uint8_t *empty)
+                             float lut_scale, uint8_t *dist)
 {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
         int lo = (int) (mc[2 * c] * lut_scale) - 1 - lut_off;
         int hi = (int) (mc[2 * c + 1] * lut_scale) + 1 - lut_off;
         lo = min(max(lo, 0), lut_n - 1);
         hi = min(max(hi, 0), lut_n - 1);
-        empty[c] = (nzprefix[hi + 1] - nzprefix[lo]) == 0 ? 1 : 0;
+        dist[c] = (nzprefix[hi + 1] - nzprefix[lo]) == 0 ? (uint8_t) kDistCap : 0;
+    }
+}
+
+// One relaxation step of the Chebyshev distance (in cells) from each
+// transparent cell to the nearest opaque one: d = min(cap, 1 + min over the
+// 26 neighbours), 0 for opaque cells; cells outside the grid count as
+// transparent (a ray there has left the brick).  After kDistCap steps d is
+// the exact distance where that is below the cap, and the cap elsewhere, so
+// every cell within d-1 of a cell with d >= 1 is transparent.  Updating in
+// place only propagates smaller values sooner, which keeps that true.
+__global__ void dist_relax_kernel(uint8_t *dist, int mcx, int mcy, int mcz)
+{
+    const int ncell = mcx * mcy * mcz;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
+        if (dist[c] == 0) continue;
+        const int x = c % mcx, y = (c / mcx) % mcy, z = c / (mcx * mcy);
+        int m = kDistCap;
+        for (int dz = -1; dz <= 1; dz++)
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int xx = x + dx, yy = y + dy, zz = z + dz;
+                    if ((dx | dy | dz) == 0 || xx < 0 || yy < 0 || zz < 0 || xx >= mcx || yy >= mcy || zz >= mcz)
+                        continue;
+                    m = min(m, (int) dist[((long long) zz * mcy + yy) * mcx + xx]);
+                }
+        dist[c] = (uint8_t) min(kDistCap, m + 1);
     }
 }
 
@@ -240,10 +267,13 @@ cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int n
     return cudaGetLastError();
 }
 
-cudaError_t launch_empty_flags(const float *mc, int ncell, const int *nzprefix, int lut_n, int lut_off,
-                               float lut_scale, uint8_t *empty, cudaStream_t s)
+cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const int *nzprefix, int lut_n,
+                               int lut_off, float lut_scale, uint8_t *empty, cudaStream_t s)
 {
+    const int ncell = mcx * mcy * mcz;
     empty_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mc, ncell, nzprefix, lut_n, lut_off, lut_scale, empty);
+    for (int it = 0; it < kDistCap; it++)
+        dist_relax_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(empty, mcx, mcy, mcz);
     return cudaGetLastError();
 }
 

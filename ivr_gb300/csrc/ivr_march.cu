@@ -17,6 +17,9 @@ namespace {
 constexpr int kBlockX = 16;  // pixels per block: 2x2 warps of 8x4
 constexpr int kBlockY = 8;
 constexpr int kThreads = 128;
+#ifndef IVR_CFG_PAIR
+#define IVR_CFG_PAIR 1  // two CONFIG samples per loop iteration
+#endif
 #ifndef IVR_CFG_BLOCKS_PER_SM
 #define IVR_CFG_BLOCKS_PER_SM 8
 #endif
@@ -43,6 +46,18 @@ __device__ __forceinline__ float vload32(const void *p, unsigned i)
 // getrayintersect (ray.c:276-318).  All six planes are visited: once
 // tin >= tout no later plane can make it a hit, so skipping the reference's
 // early loop exit changes nothing.
+// numer = d - n.o and denom = n.d for face p (normals of aabb.facenormals,
+// main.c:611-613), evaluated as dot3f does.
+__device__ __forceinline__ void plane_eval(int p, float dc, float ox, float oy, float oz, float dx, float dy,
+                                           float dz, float &numer, float &denom)
+{
+    const int axis = p >> 1;
+    const float nrm = (p & 1) ? 1.0f : -1.0f;
+    const float nx = axis == 0 ? nrm : 0.0f, ny = axis == 1 ? nrm : 0.0f, nz = axis == 2 ? nrm : 0.0f;
+    numer = dc - (nx * ox + ny * oy + nz * oz);
+    denom = nx * dx + ny * dy + nz * dz;
+}
+
 __device__ __forceinline__ bool ray_box(const float *dc, float ox, float oy, float oz, float dx, float dy,
                                         float dz, float &tin, float &tout)
 {
@@ -50,11 +65,8 @@ __device__ __forceinline__ bool ray_box(const float *dc, float ox, float oy, flo
     tout = FLT_MAX;
 #pragma unroll
     for (int p = 0; p < 6; p++) {
-        const int axis = p >> 1;
-        const float nrm = (p & 1) ? 1.0f : -1.0f;
-        const float nx = axis == 0 ? nrm : 0.0f, ny = axis == 1 ? nrm : 0.0f, nz = axis == 2 ? nrm : 0.0f;
-        float numer = dc[p] - (nx * ox + ny * oy + nz * oz);
-        float denom = nx * dx + ny * dy + nz * dz;
+        float numer, denom;
+        plane_eval(p, dc[p], ox, oy, oz, dx, dy, dz, numer, denom);
         if (tin < tout) {
             if (denom == 0.0f) {
                 if (numer < 0.0f) tin = tout + 1.0f;
@@ -126,9 +138,9 @@ __device__ __forceinline__ float sample_cfg(const DevBrick &b, float x, float y,
     float ux = (x - b.bminx) * b.icx;
     float uy = (y - b.bminy) * b.icy;
     float uz = (z - b.bminz) * b.icz;
-    int j = min(max((int) floorf(ux), 0), nx - 2);
-    int i = min(max((int) floorf(uy), 0), ny - 2);
-    int k = min(max((int) floorf(uz), 0), nz - 2);
+    int j = min(max(__float2int_rd(ux), 0), nx - 2);
+    int i = min(max(__float2int_rd(uy), 0), ny - 2);
+    int k = min(max(__float2int_rd(uz), 0), nz - 2);
     float fx = fminf(fmaxf(ux - (float) j, 0.0f), 1.0f);
     float fy = fminf(fmaxf(uy - (float) i, 0.0f), 1.0f);
     float fz = fminf(fmaxf(uz - (float) k, 0.0f), 1.0f);
@@ -269,21 +281,16 @@ __device__ __forceinline__ float cfg_t(float t0, float dt, int i) { return fmaf(
 // First lattice index i >= 0 with t_i >= a.  The estimate is exact up to
 // rounding, so the fix-up loops run a step or two; they are bounded anyway.
 constexpr int kMaxLattice = 1 << 24;
-__device__ __forceinline__ int cfg_first_ge(float t0, float dt, float a)
+__device__ __forceinline__ int cfg_first_ge(float t0, float dt, float idt, float a)
 {
     if (!(a > t0)) return 0;
-    float q = (a - t0) / dt;
+    float q = (a - t0) * idt;  // an estimate: the loops below make it exact
     int i = q < (float) kMaxLattice ? (int) q : kMaxLattice;
     for (int it = 0; it < 64 && i > 0 && cfg_t(t0, dt, i - 1) >= a; it++) i--;
     for (int it = 0; it < 64 && i < kMaxLattice && cfg_t(t0, dt, i) < a; it++) i++;
     return i;
 }
 
-// Is macrocell (ci,cj,ck) of a brick transparent under the current TF?
-__device__ __forceinline__ bool cell_empty(const DevBrick &b, int ci, int cj, int ck)
-{
-    return b.empty[((long long) ck * b.mcy + ci) * b.mcx + cj] != 0;
-}
 
 // One brick of the CONFIG march: samples tin_k <= t_i < tout_k of the ray's
 // lattice, front-to-back into acc.  One loop iteration is one lattice index
@@ -302,8 +309,8 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float
 {
     float tin, tout;
     if (!ray_box(b.dconst, f.origx, f.origy, f.origz, dx, dy, dz, tin, tout)) return;
-    const int i0 = cfg_first_ge(t0, dt, tin);
-    const int i1 = cfg_first_ge(t0, dt, tout);
+    const int i0 = cfg_first_ge(t0, dt, idt, tin);
+    const int i1 = cfg_first_ge(t0, dt, idt, tout);
     if (CENSUS) {
         nlat += (unsigned long long) max(i1 - i0, 0);
         if (done) return;
@@ -315,25 +322,64 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float
         const float t = cfg_t(t0, dt, i);
         const float x = fmaf(dx, t, ox), y = fmaf(dy, t, oy), z = fmaf(dz, t, oz);
         if (SKIP && i >= icheck) {
-            const int cj = min(max((int) floorf((x - b.bminx) * b.icx), 0), b.nx - 2) / kCell;
-            const int ci = min(max((int) floorf((y - b.bminy) * b.icy), 0), b.ny - 2) / kCell;
-            const int ck = min(max((int) floorf((z - b.bminz) * b.icz), 0), b.nz - 2) / kCell;
-            // ray parameter where it leaves the cell's box (approximate:
-            // the margins absorb its rounding)
-            const float tx = dx > 0.0f ? (fmaf((float) (cj + 1), b.mcwx, b.bminx) - ox) * idx
-                             : dx < 0.0f ? (fmaf((float) cj, b.mcwx, b.bminx) - ox) * idx : FLT_MAX;
-            const float ty = dy > 0.0f ? (fmaf((float) (ci + 1), b.mcwy, b.bminy) - oy) * idy
-                             : dy < 0.0f ? (fmaf((float) ci, b.mcwy, b.bminy) - oy) * idy : FLT_MAX;
-            const float tz = dz > 0.0f ? (fmaf((float) (ck + 1), b.mcwz, b.bminz) - oz) * idz
-                             : dz < 0.0f ? (fmaf((float) ck, b.mcwz, b.bminz) - oz) * idz : FLT_MAX;
+            const int cj = min(max(__float2int_rd((x - b.bminx) * b.icx), 0), b.nx - 2) / kCell;
+            const int ci = min(max(__float2int_rd((y - b.bminy) * b.icy), 0), b.ny - 2) / kCell;
+            const int ck = min(max(__float2int_rd((z - b.bminz) * b.icz), 0), b.nz - 2) / kCell;
+            // r >= 1: the cube of cells within r-1 of this one is transparent
+            const int r = b.empty[((long long) ck * b.mcy + ci) * b.mcx + cj];
+            const int rr = max(r, 1);
+            // ray parameter where it leaves that cube (or this one opaque
+            // cell); approximate, the margins absorb its rounding
+            const float tx = dx > 0.0f ? (fmaf((float) (cj + rr), b.mcwx, b.bminx) - ox) * idx
+                             : dx < 0.0f ? (fmaf((float) (cj - rr + 1), b.mcwx, b.bminx) - ox) * idx : FLT_MAX;
+            const float ty = dy > 0.0f ? (fmaf((float) (ci + rr), b.mcwy, b.bminy) - oy) * idy
+                             : dy < 0.0f ? (fmaf((float) (ci - rr + 1), b.mcwy, b.bminy) - oy) * idy : FLT_MAX;
+            const float tz = dz > 0.0f ? (fmaf((float) (ck + rr), b.mcwz, b.bminz) - oz) * idz
+                             : dz < 0.0f ? (fmaf((float) (ck - rr + 1), b.mcwz, b.bminz) - oz) * idz : FLT_MAX;
             const float q = fminf(fmaxf((fminf(tx, fminf(ty, tz)) - t0) * idt, 0.0f), (float) kMaxLattice);
             const int iexit = (int) q;  // last lattice index at or before the exit
-            if (cell_empty(b, ci, cj, ck)) {
+            if (r != 0) {
                 i = max(i, iexit - 2);  // the loop's ++ resumes at iexit - 1
                 continue;
             }
             icheck = iexit + 1;
         }
+#if IVR_CFG_PAIR
+        // two samples per iteration: both samples' loads are in flight
+        // before either is composited.  The second is only composited when
+        // it comes before the next cell check and the first did not end the
+        // ray; sample_cfg clamps its indices, so computing it is always safe.
+        if (!CENSUS) {
+            const int lim = SKIP ? min(i1, icheck) : i1;
+            const float t1 = cfg_t(t0, dt, i + 1);
+            const float s0 = sample_cfg<DT>(b, x, y, z);
+            const float s1 = sample_cfg<DT>(b, fmaf(dx, t1, ox), fmaf(dy, t1, oy), fmaf(dz, t1, oz));
+            const float4 e0 = lut_at(f, (int) (s0 * f.lut_scale) - f.lut_off);
+            const float4 e1 = lut_at(f, (int) (s1 * f.lut_scale) - f.lut_off);
+            float wgt = (1.0f - acc.w) * (e0.w * opac);
+            acc.x = fmaf(wgt, e0.x, acc.x);
+            acc.y = fmaf(wgt, e0.y, acc.y);
+            acc.z = fmaf(wgt, e0.z, acc.z);
+            acc.w = acc.w + wgt;
+            if (acc.w >= term) {
+                done = true;
+                return;
+            }
+            if (i + 1 < lim) {
+                wgt = (1.0f - acc.w) * (e1.w * opac);
+                acc.x = fmaf(wgt, e1.x, acc.x);
+                acc.y = fmaf(wgt, e1.y, acc.y);
+                acc.z = fmaf(wgt, e1.z, acc.z);
+                acc.w = acc.w + wgt;
+                if (acc.w >= term) {
+                    done = true;
+                    return;
+                }
+                i++;
+            }
+            continue;
+        }
+#endif
         const float s = sample_cfg<DT>(b, x, y, z);
         if (CENSUS) {
             nexec++;
@@ -504,7 +550,7 @@ __global__ void __launch_bounds__(kThreads, kCfgBlocksPerSm) march_cfg_kernel(co
 }
 
 template <typename K>
-int persistent_grid(K kernel)
+int persistent_grid(K kernel, size_t smem)
 {
     static int sms = 0;
     if (sms == 0) {
@@ -513,7 +559,7 @@ int persistent_grid(K kernel)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     }
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
     return sms * (per_sm > 0 ? per_sm : 1);
 }
 
@@ -526,14 +572,15 @@ cudaError_t launch_dt(const FrameDesc &f, float4 *o32, uchar4 *o8, cudaStream_t 
         for (int k = 0; k < f.nb; k++) skip |= f.b[k].empty != nullptr;
         auto kern = f.census ? (skip ? march_cfg_kernel<DT, true, true> : march_cfg_kernel<DT, false, true>)
                              : (skip ? march_cfg_kernel<DT, true, false> : march_cfg_kernel<DT, false, false>);
+        const size_t smem = 0;
 #if IVR_CFG_PERSISTENT
-        const int blocks = persistent_grid(kern);
+        const int blocks = persistent_grid(kern, smem);
         // every tile is taken once and every warp ends on one failed take
         if (warps_launched)
             *warps_launched = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2) + (long long) blocks * (kThreads / 32);
-        kern<<<blocks, kThreads, 0, s>>>(f, o32, o8);
+        kern<<<blocks, kThreads, smem, s>>>(f, o32, o8);
 #else
-        kern<<<grid, kThreads, 0, s>>>(f, o32, o8);
+        kern<<<grid, kThreads, smem, s>>>(f, o32, o8);
 #endif
         return cudaGetLastError();
     }
