@@ -142,6 +142,22 @@ int ivr_bricks_setup(ivr_volume *vol, int py, int px, int pz, int overlap);
  * otherwise it holds hsize = (int)(max-min+1) bins). */
 int ivr_volume_minmax(ivr_volume *vol, float *mn, float *mx);
 int ivr_volume_histogram(ivr_volume *vol, int *hist, int hsize);
+/* The same min, max and histogram without allocating any device memory.
+ * This entry point has no counterpart in the reference.  It is for callers
+ * that must not call cudaMalloc/cudaFree here: a steering server whose HBM
+ * budget is fully given to resident volumes, a frame loop that cannot take
+ * the device-wide synchronisation cudaFree implies while other streams are
+ * rendering, or code that runs while a stream is being captured.  Its
+ * scratch is one static device array (about 261 KiB) that every GPU loading
+ * this library holds until the process exits, so hsize is limited to
+ * 65536 bins (IVR_ERR_INVALID above that).  The first call on a device looks
+ * up that array's address (and loads the library's kernels there if they
+ * are not loaded yet): make it before any stream capture.  Calls share the
+ * array and it keeps the last call's contents (the bins are cleared at the
+ * start of each call): calls that overlap on the GPU -- on two streams or
+ * from two threads -- race.  Outputs are host memory; the call waits for
+ * them on `stream`. */
+int ivr_volume_histogram_noalloc(ivr_volume *vol, int *hist, int hsize, float *mn, float *mx, void *stream);
 
 /* --- transfer function (initcolormap, initvolluts, inittransferfunc) ---- */
 int ivr_tf_create(ivr_ctx *ctx, ivr_tf **out);

@@ -62,6 +62,7 @@ SIGNATURES = {
     "ivr_bricks_setup": (_I, [_P, _I, _I, _I, _I]),
     "ivr_volume_minmax": (_I, [_P, _PF, _PF]),
     "ivr_volume_histogram": (_I, [_P, _PI, _I]),
+    "ivr_volume_histogram_noalloc": (_I, [_P, _PI, _I, _PF, _PF, _P]),
     "ivr_tf_create": (_I, [_P, ctypes.POINTER(_P)]),
     "ivr_tf_free": (_I, [_P]),
     "ivr_tf_set_lut": (_I, [_P, _PF, _I, _I, _F, _I]),

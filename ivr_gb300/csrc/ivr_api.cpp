@@ -437,6 +437,23 @@ int ivr_volume_histogram(ivr_volume *v, int *hist, int hsize)
     return IVR_OK;
 }
 
+int ivr_volume_histogram_noalloc(ivr_volume *v, int *hist, int hsize, float *mn, float *mx, void *stream)
+{
+    if (!v) return IVR_ERR_INVALID;
+    ivr_ctx *c = v->ctx;
+    if (!hist || !mn || !mx) return fail(c, IVR_ERR_INVALID, "null output");
+    if (hsize < 1 || hsize > kNoAllocMaxBins)
+        return fail(c, IVR_ERR_INVALID, "hsize %d is outside [1, %d], the bins the allocation-free histogram holds",
+                    hsize, kNoAllocMaxBins);
+    CK(c, cudaSetDevice(c->device));
+    float mm[2];
+    CK(c, noalloc_histogram(v->d_full, v->dtype, (long long) v->w * v->h * v->d, hsize, hist, mm,
+                            (cudaStream_t) stream));
+    *mn = mm[0];
+    *mx = mm[1];
+    return IVR_OK;
+}
+
 int ivr_tf_create(ivr_ctx *c, ivr_tf **out)
 {
     if (!c || !out) return IVR_ERR_INVALID;

@@ -98,6 +98,12 @@ cudaError_t launch_composite(float *dst, const float *src, int num, long long np
 cudaError_t launch_quantize(const float *in, uint8_t *out, long long n, cudaStream_t s);
 int minmax_parts();
 
+// allocation-free histogram (ivr_volume_histogram_noalloc): min/max and
+// hsize <= kNoAllocMaxBins bins of n voxels, scratch in a static device array
+constexpr int kNoAllocMaxBins = 65536;
+cudaError_t noalloc_histogram(const void *data, int dtype, long long n, int hsize, int *hist_host,
+                              float *minmax_host, cudaStream_t s);
+
 // march (ivr_march.cu)
 // *tickets: how many tile tickets the launch takes from f.tickets (a
 // persistent CONFIG launch takes each tile once and each warp fails once).

@@ -5,6 +5,8 @@
 #include <float.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "ivr_internal.h"
 
 namespace ivr {
@@ -219,7 +221,104 @@ __global__ void quantize_kernel(const float *__restrict__ in, uint8_t *__restric
         out[i] = (uint8_t) q8k(in[i]);
 }
 
+// ---- allocation-free histogram ---------------------------------------------
+// Scratch of ivr_volume_histogram_noalloc: min/max partials, the reduced
+// min/max and up to kNoAllocMaxBins bins, in one static device array that
+// every GPU loading this library holds until the process exits.
+struct NoAllocScratch {
+    float partial[2 * kSms * 4];
+    float minmax[2];
+    int hist[kNoAllocMaxBins];
+};
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+__global__ void minmax_final_kernel(const float *partial, int nparts, float *minmax)
+{
+    float lo = FLT_MAX, hi = -FLT_MAX;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+        lo = fminf(lo, partial[2 * i]);
+        hi = fmaxf(hi, partial[2 * i + 1]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    __shared__ float slo[32], shi[32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { slo[w] = lo; shi[w] = hi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int) (blockDim.x >> 5); k++) { lo = fminf(lo, slo[k]); hi = fmaxf(hi, shi[k]); }
+        minmax[0] = lo;
+        minmax[1] = hi;
+    }
+}
+
+// the histogram of hist_*_kernel with the minimum read from device memory
+__global__ void hist_devmin_kernel(const void *data, int dtype, long long n, const float *minmax, int hsize,
+                                   int *hist)
+{
+    __shared__ int sh[kSmemBins];
+    const float mn = minmax[0];
+    const bool priv = hsize <= kSmemBins;
+    if (priv) {
+        for (int b = threadIdx.x; b < hsize; b += blockDim.x) sh[b] = 0;
+        __syncthreads();
+    }
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        int b = (int) (load_any(data, dtype, i) - mn);
+        if (b >= 0 && b < hsize) atomicAdd(priv ? &sh[b] : &hist[b], 1);
+    }
+    if (priv) {
+        __syncthreads();
+        for (int b = threadIdx.x; b < hsize; b += blockDim.x)
+            if (sh[b]) atomicAdd(&hist[b], sh[b]);
+    }
+}
+
 }  // namespace
+
+// Device address of the static scratch on the current device.  Resolved
+// once per device with cudaGetSymbolAddress (the first call on a device
+// loads this module there if it is not loaded yet).
+static cudaError_t noalloc_scratch(NoAllocScratch **out)
+{
+    static std::mutex mu;
+    static void *ptrs[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptrs[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        ptrs[dev] = p;
+    }
+    *out = static_cast<NoAllocScratch *>(ptrs[dev]);
+    return cudaSuccess;
+}
+
+cudaError_t noalloc_histogram(const void *data, int dtype, long long n, int hsize, int *hist_host,
+                              float *minmax_host, cudaStream_t s)
+{
+    NoAllocScratch *sc = nullptr;
+    cudaError_t e = noalloc_scratch(&sc);
+    if (e != cudaSuccess) return e;
+    const int parts = kSms * 4;
+    minmax_kernel<<<parts, 256, 0, s>>>(data, dtype, n, sc->partial);
+    minmax_final_kernel<<<1, 1024, 0, s>>>(sc->partial, parts, sc->minmax);
+    if ((e = cudaMemsetAsync(sc->hist, 0, sizeof(int) * (size_t) hsize, s)) != cudaSuccess) return e;
+    hist_devmin_kernel<<<grid_for(n, 512, 2), 512, 0, s>>>(data, dtype, n, sc->minmax, hsize, sc->hist);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(hist_host, sc->hist, sizeof(int) * (size_t) hsize, cudaMemcpyDeviceToHost, s)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaMemcpyAsync(minmax_host, sc->minmax, 2 * sizeof(float), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return e;
+    return cudaStreamSynchronize(s);
+}
 
 size_t dtype_size(int dtype) { return dtype == IVR_U8 ? 1 : dtype == IVR_U16 ? 2 : 4; }
 
