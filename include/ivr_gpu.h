@@ -199,6 +199,28 @@ int ivr_render_host(ivr_view *view, ivr_volume *vol, ivr_tf *tf, const ivr_state
 int ivr_census(ivr_view *view, ivr_tf *tf, unsigned long long *lattice, unsigned long long *executed,
                unsigned long long *touched_bytes, void *stream);
 
+/* --- batches: many frames in one persistent launch ---------------------- */
+/* A batch holds up to max_frames CONFIG frames (each a set view, a TF and
+ * its output buffers) of volumes with one dtype; ivr_batch_render renders
+ * them all in one persistent launch (warps take tiles of every frame from
+ * one queue).  With use_graph the launch is captured into a CUDA graph on
+ * first use and replayed after that.  Each frame is bitwise the frame
+ * ivr_render gives for the same view and TF.  The batch's staging memory is
+ * reused: ivr_batch_clear/ivr_batch_add wait until the last render has
+ * started reading it. */
+typedef struct ivr_batch ivr_batch;
+int ivr_batch_create(ivr_ctx *ctx, int max_frames, ivr_batch **out);
+int ivr_batch_free(ivr_batch *batch);
+int ivr_batch_clear(ivr_batch *batch);
+int ivr_batch_add(ivr_batch *batch, ivr_view *view, ivr_tf *tf, float *rgba32_dev, uint8_t *rgba8_dev);
+int ivr_batch_render(ivr_batch *batch, int use_graph, void *stream);
+/* Times every kernel variant (warp tiles 8x4, 4x8, 16x2; one or two
+ * samples per loop iteration) on the filled batch and keeps the fastest.
+ * variant (nullable) receives its index, ms_per_variant (nullable, 6 floats)
+ * the timings. */
+int ivr_batch_autotune(ivr_batch *batch, void *stream, int *variant, float *ms_per_variant);
+int ivr_batch_set_variant(ivr_batch *batch, int variant);
+
 /* --- compositing and output -------------------------------------------- */
 /* compositetiles (main.c:1203-1218): num sub-images of w*h RGBA floats in
  * near -> far order, composited far -> near onto tilebuf with

@@ -78,6 +78,13 @@ SIGNATURES = {
     "ivr_render_host": (_I, [_P, _P, _P, ctypes.POINTER(IvrState), ctypes.POINTER(RenderParams), _P, _P]),
     "ivr_census": (_I, [_P, _P, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong),
                         ctypes.POINTER(ctypes.c_ulonglong), _P]),
+    "ivr_batch_create": (_I, [_P, _I, ctypes.POINTER(_P)]),
+    "ivr_batch_free": (_I, [_P]),
+    "ivr_batch_clear": (_I, [_P]),
+    "ivr_batch_add": (_I, [_P, _P, _P, _P, _P]),
+    "ivr_batch_render": (_I, [_P, _I, _P]),
+    "ivr_batch_autotune": (_I, [_P, _P, ctypes.POINTER(_I), _PF]),
+    "ivr_batch_set_variant": (_I, [_P, _I]),
     "ivr_composite": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "ivr_quantize": (_I, [_P, _P, _P, ctypes.c_longlong, _P]),
 }

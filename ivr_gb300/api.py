@@ -108,6 +108,11 @@ class Context:
         self.check(self.lib.ivr_view_create(self.h, ctypes.byref(out)))
         return View(self, out)
 
+    def batch(self, max_frames: int) -> "Batch":
+        out = ctypes.c_void_p()
+        self.check(self.lib.ivr_batch_create(self.h, max_frames, ctypes.byref(out)))
+        return Batch(self, out)
+
     def composite(self, tilebuf, rcolorbuf, num: int, w: int, h: int, stream=None):
         """compositetiles: num w*h RGBA sub-images (near -> far) over tilebuf."""
         self.check(self.lib.ivr_composite(self.h, _vp(tilebuf), _vp(rcolorbuf), num, w, h, _vp(stream)))
@@ -217,4 +222,36 @@ class View:
     def free(self):
         if self.h:
             self.ctx.lib.ivr_view_free(self.h)
+            self.h = None
+
+
+class Batch:
+    """Many CONFIG frames in one persistent launch (ivr_batch_*)."""
+
+    VARIANTS = ["8x4 pair", "8x4", "4x8 pair", "4x8", "16x2 pair", "16x2"]
+
+    def __init__(self, ctx: Context, h):
+        self.ctx, self.h = ctx, h
+
+    def clear(self):
+        self.ctx.check(self.ctx.lib.ivr_batch_clear(self.h))
+
+    def add(self, view: View, tf: TransferFunction, rgba32=None, rgba8=None):
+        self.ctx.check(self.ctx.lib.ivr_batch_add(self.h, view.h, tf.h, _vp(rgba32), _vp(rgba8)))
+
+    def render(self, use_graph: bool = False, stream=None):
+        self.ctx.check(self.ctx.lib.ivr_batch_render(self.h, int(use_graph), _vp(stream)))
+
+    def autotune(self, stream=None):
+        v = ctypes.c_int()
+        ms = (ctypes.c_float * 6)()
+        self.ctx.check(self.ctx.lib.ivr_batch_autotune(self.h, _vp(stream), ctypes.byref(v), ms))
+        return v.value, list(ms)
+
+    def set_variant(self, v: int):
+        self.ctx.check(self.ctx.lib.ivr_batch_set_variant(self.h, v))
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.ivr_batch_free(self.h)
             self.h = None

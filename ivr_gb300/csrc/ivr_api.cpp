@@ -34,9 +34,18 @@ struct ivr_volume {
     int py = 1, px = 1, pz = 1, overlap = 0;
     bool have_minmax = false;
     float vmin = 0.0f, vmax = 0.0f;
-    unsigned empty_serial = 0;  // TF serial the empty flags were built for
-    int empty_zero_alpha = -1;  // whether they were built for alpha == 0
+    // macrocell distance fields, one set per transfer function in use
+    // (keyed by TF serial and whether the opacity scale is zero)
+    struct TfGrid {
+        unsigned serial;
+        int zero_alpha;
+        unsigned long long last_use;
+        std::vector<uint8_t *> dist;  // per brick
+    };
+    std::vector<TfGrid> grids;
+    unsigned long long use_clock = 0;
 };
+constexpr size_t kMaxTfGrids = 16;
 
 struct ivr_tf {
     ivr_ctx *ctx = nullptr;
@@ -60,6 +69,20 @@ struct ivr_view {
     bool valid = false;
     ivr::FrameDesc f{};
     ivr_frame_info info{};
+};
+
+struct ivr_batch {
+    ivr_ctx *ctx = nullptr;
+    int cap = 0, n = 0, dtype = -1;
+    int variant = 0;
+    void *h_buf = nullptr;  // pinned: BatchHeader then cap BatchItems
+    void *d_buf = nullptr;
+    size_t buf_bytes = 0;
+    unsigned long long *d_ticket = nullptr;
+    cudaEvent_t done = nullptr;  // after the last render: the staging may be refilled
+    bool pending = false;
+    cudaGraphExec_t graph[ivr::kBatchVariants] = {};
+    cudaStream_t graph_stream[ivr::kBatchVariants] = {};
 };
 
 namespace {
@@ -120,16 +143,21 @@ size_t brick_bytes(const ivr_volume *v, const HostBrick &b)
 
 size_t mc_cells(const HostBrick &b) { return (size_t) b.mcx * b.mcy * b.mcz; }
 
+void free_grids(ivr_volume *v)
+{
+    for (auto &g : v->grids)
+        for (size_t k = 0; k < g.dist.size(); k++) dev_free(v->ctx, g.dist[k], mc_cells(v->bricks[k]));
+    v->grids.clear();
+}
+
 void free_bricks(ivr_volume *v)
 {
+    free_grids(v);
     for (auto &b : v->bricks) {
         if (b.owns) dev_free(v->ctx, b.data, brick_bytes(v, b));
         dev_free(v->ctx, b.mc_minmax, mc_cells(b) * 2 * sizeof(float));
-        dev_free(v->ctx, b.empty, mc_cells(b));
     }
     v->bricks.clear();
-    v->empty_serial = 0;
-    v->empty_zero_alpha = -1;
 }
 
 // macrocell grid over a brick's local voxels (cells of kCell, +1 layer)
@@ -139,8 +167,6 @@ int build_macrocells(ivr_volume *v, HostBrick &b)
     b.mcy = (b.lh - 2) / kCell + 1;
     b.mcz = (b.ld - 2) / kCell + 1;
     int rc = dev_alloc(v->ctx, mc_cells(b) * 2 * sizeof(float), (void **) &b.mc_minmax);
-    if (rc) return rc;
-    rc = dev_alloc(v->ctx, mc_cells(b), (void **) &b.empty);
     if (rc) return rc;
     CK(v->ctx, launch_macrocells(b.data, v->dtype, b.lw, b.lh, b.ld, b.mc_minmax, b.mcx, b.mcy, b.mcz, 0));
     return IVR_OK;
@@ -196,27 +222,63 @@ int valid_params(ivr_ctx *c, const ivr_render_params *p)
     return IVR_OK;
 }
 
-// Per-brick empty-cell flags for a TF (cached by TF serial and by whether
-// the opacity scale is zero).
-int refresh_empty(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s)
+// The per-brick distance fields of the volume for a TF, built on `s` when
+// the TF (or a zero opacity scale) is new to the volume.  Up to kMaxTfGrids
+// are kept; the least recently used is rebuilt in place, after the device
+// has finished every launch that may still read it.
+int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s, const std::vector<uint8_t *> **out,
+            bool *built = nullptr)
 {
-    if (v->empty_serial == tf->serial && v->empty_zero_alpha == (int) zero_alpha) return IVR_OK;
-    for (auto &b : v->bricks) {
-        if (zero_alpha) CK(v->ctx, cudaMemsetAsync(b.empty, kDistCap, mc_cells(b), s));
-        else CK(v->ctx, launch_empty_flags(b.mc_minmax, b.mcx, b.mcy, b.mcz, tf->d_nzprefix, tf->n, tf->off,
-                                           tf->scale, b.empty, s));
+    if (built) *built = false;
+    ivr_ctx *c = v->ctx;
+    const unsigned long long now = ++v->use_clock;
+    for (auto &g : v->grids)
+        if (g.serial == tf->serial && g.zero_alpha == (int) zero_alpha) {
+            g.last_use = now;
+            *out = &g.dist;
+            return IVR_OK;
+        }
+    ivr_volume::TfGrid *g = nullptr;
+    if (v->grids.size() < kMaxTfGrids) {
+        v->grids.push_back(ivr_volume::TfGrid{0, 0, 0, std::vector<uint8_t *>(v->bricks.size(), nullptr)});
+        g = &v->grids.back();
+        for (size_t k = 0; k < v->bricks.size(); k++) {
+            int rc = dev_alloc(c, mc_cells(v->bricks[k]), (void **) &g->dist[k]);
+            if (rc) {
+                for (size_t j = 0; j < k; j++) dev_free(c, g->dist[j], mc_cells(v->bricks[j]));
+                v->grids.pop_back();
+                return rc;
+            }
+        }
+    } else {
+        g = &v->grids[0];
+        for (auto &h : v->grids)
+            if (h.last_use < g->last_use) g = &h;
+        CK(c, cudaDeviceSynchronize());
     }
-    v->empty_serial = tf->serial;
-    v->empty_zero_alpha = (int) zero_alpha;
+    g->serial = tf->serial;
+    g->zero_alpha = (int) zero_alpha;
+    g->last_use = now;
+    for (size_t k = 0; k < v->bricks.size(); k++) {
+        const HostBrick &b = v->bricks[k];
+        if (zero_alpha) CK(c, cudaMemsetAsync(g->dist[k], kDistCap, mc_cells(b), s));
+        else CK(c, launch_empty_flags(b.mc_minmax, b.mcx, b.mcy, b.mcz, tf->d_nzprefix, tf->n, tf->off, tf->scale,
+                                      g->dist[k], s));
+    }
+    *out = &g->dist;
+    if (built) *built = true;
     return IVR_OK;
 }
 
-int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single, float *o32, uint8_t *o8,
-                  void *stream, std::vector<uint8_t *> *touched = nullptr)
+// Fills everything of a launch's frame descriptor that depends on the TF,
+// the output window and the skipping grid.
+int frame_for(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single, cudaStream_t s, FrameDesc &f,
+              bool *built = nullptr)
 {
-    ivr_ctx *c = view ? view->ctx : nullptr;
-    if (!view || !tf) return fail(c, IVR_ERR_INVALID, "null view or transfer function");
+    if (built) *built = false;
+    ivr_ctx *c = view->ctx;
     if (!view->valid) return fail(c, IVR_ERR_INVALID, "ivr_set_view has not succeeded on this view");
+    if (!tf) return fail(c, IVR_ERR_INVALID, "null transfer function");
     if (tf->mode != IVR_TF_RGBBLEND && tf->n < 1) return fail(c, IVR_ERR_INVALID, "transfer function has no LUT");
     const bool f2b = tf->mode == IVR_TF_F2B;
     if ((view->p.preset == IVR_PRESET_CONFIG) != f2b)
@@ -224,8 +286,7 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
     if (x < 0 || y < 0 || w < 1 || h < 1 || x + w > view->info.vw || y + h > view->info.vh)
         return fail(c, IVR_ERR_INVALID, "tile %d,%d %dx%d outside the %dx%d viewport", x, y, w, h, view->info.vw,
                     view->info.vh);
-    cudaStream_t s = (cudaStream_t) stream;
-    FrameDesc f = view->f;
+    f = view->f;
     f.tf_mode = tf->mode;
     f.lut = tf->d_lut;
     f.lut_n = tf->n;
@@ -233,13 +294,26 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
     f.lut_scale = tf->scale;
     f.out_x = x; f.out_y = y; f.out_w = w; f.out_h = h;
     f.single = single;
-    f.counters = touched ? c->d_counters : nullptr;  // census launches count
-    const bool skip = view->p.skip == IVR_SKIP_GRID && view->p.preset == IVR_PRESET_CONFIG;
-    if (skip) {
-        int rc = refresh_empty(view->vol, tf, !(f.alpha != 0.0f), s);
+    f.counters = nullptr;
+    if (view->p.skip == IVR_SKIP_GRID && view->p.preset == IVR_PRESET_CONFIG) {
+        const std::vector<uint8_t *> *dist = nullptr;
+        int rc = tf_grid(view->vol, tf, !(f.alpha != 0.0f), s, &dist, built);
         if (rc) return rc;
-        for (int k = 0; k < f.nb; k++) f.b[k].empty = view->vol->bricks[k].empty;
+        for (int k = 0; k < f.nb; k++) f.b[k].empty = (*dist)[k];
     }
+    return IVR_OK;
+}
+
+int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single, float *o32, uint8_t *o8,
+                  void *stream, std::vector<uint8_t *> *touched = nullptr)
+{
+    ivr_ctx *c = view ? view->ctx : nullptr;
+    if (!view) return fail(c, IVR_ERR_INVALID, "null view");
+    cudaStream_t s = (cudaStream_t) stream;
+    FrameDesc f;
+    int rc = frame_for(view, tf, x, y, w, h, single, s, f);
+    if (rc) return rc;
+    if (touched) f.counters = c->d_counters;  // census launches count
     if (touched) {
         f.census = 1;
         for (int k = 0; k < f.nb; k++) f.b[k].touched = (*touched)[k];
@@ -665,6 +739,213 @@ int ivr_census(ivr_view *view, ivr_tf *tf, unsigned long long *lattice, unsigned
     if (lattice) *lattice = cnt[1];
     if (executed) *executed = cnt[0];
     if (touched_bytes) *touched_bytes = bytes;
+    return IVR_OK;
+}
+
+// --- batches -----------------------------------------------------------
+namespace {
+size_t batch_bytes(int cap) { return sizeof(BatchHeader) + sizeof(BatchItem) * (size_t) cap; }
+BatchHeader *batch_hdr(ivr_batch *b) { return (BatchHeader *) b->h_buf; }
+BatchItem *batch_items(ivr_batch *b) { return (BatchItem *) ((char *) b->h_buf + sizeof(BatchHeader)); }
+
+int batch_wait(ivr_batch *b)
+{
+    if (b->pending) {
+        CK(b->ctx, cudaEventSynchronize(b->done));
+        b->pending = false;
+    }
+    return IVR_OK;
+}
+
+// tile numbering for the batch's warp-tile width
+void batch_layout(ivr_batch *b)
+{
+    const int tw = batch_variant_tile_w(b->variant), th = 32 / tw;
+    long long t = 0;
+    BatchItem *it = batch_items(b);
+    for (int i = 0; i < b->n; i++) {
+        it[i].tile0 = t;
+        it[i].tiles_x = (it[i].f.out_w + tw - 1) / tw;
+        t += (long long) it[i].tiles_x * ((it[i].f.out_h + th - 1) / th);
+    }
+    batch_hdr(b)->nitems = b->n;
+    batch_hdr(b)->total_tiles = t;
+}
+
+int batch_launch(ivr_batch *b, cudaStream_t s, bool graph)
+{
+    ivr_ctx *c = b->ctx;
+    if (!graph) {
+        CK(c, cudaMemsetAsync(b->d_ticket, 0, sizeof(unsigned long long), s));
+        CK(c, cudaMemcpyAsync(b->d_buf, b->h_buf, batch_bytes(b->n), cudaMemcpyHostToDevice, s));
+        CK(c, launch_batch(b->dtype, b->variant, (const BatchHeader *) b->d_buf,
+                           (const BatchItem *) ((char *) b->d_buf + sizeof(BatchHeader)), b->d_ticket, s));
+        return IVR_OK;
+    }
+    const int v = b->variant;
+    if (!b->graph[v]) {
+        // capture once: ticket reset, descriptor upload (the whole staging
+        // area, so any later batch of up to cap frames replays unchanged),
+        // the persistent launch
+        cudaStream_t cs;
+        CK(c, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaGraph_t g;
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->d_ticket, 0, sizeof(unsigned long long), cs);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_buf, b->h_buf, batch_bytes(b->cap), cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess)
+            e = launch_batch(b->dtype, v, (const BatchHeader *) b->d_buf,
+                             (const BatchItem *) ((char *) b->d_buf + sizeof(BatchHeader)), b->d_ticket, cs);
+        cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[v], g, 0);
+        if (e2 == cudaSuccess) cudaGraphDestroy(g);
+        cudaStreamDestroy(cs);
+        if (e != cudaSuccess) {
+            b->graph[v] = nullptr;
+            return cuda_fail(c, e, "batch graph capture");
+        }
+    }
+    CK(c, cudaGraphLaunch(b->graph[v], s));
+    return IVR_OK;
+}
+}  // namespace
+
+int ivr_batch_create(ivr_ctx *c, int max_frames, ivr_batch **out)
+{
+    if (!c || !out) return IVR_ERR_INVALID;
+    *out = nullptr;
+    if (max_frames < 1 || max_frames > 4096) return fail(c, IVR_ERR_INVALID, "batch capacity %d", max_frames);
+    ivr_batch *b = new ivr_batch();
+    b->ctx = c;
+    b->cap = max_frames;
+    b->buf_bytes = batch_bytes(max_frames);
+    cudaError_t e = cudaMallocHost(&b->h_buf, b->buf_bytes);
+    if (e != cudaSuccess) {
+        delete b;
+        return fail(c, IVR_ERR_NOMEM, "pinned staging for %d frames: %s", max_frames, cudaGetErrorString(e));
+    }
+    memset(b->h_buf, 0, b->buf_bytes);
+    int rc = dev_alloc(c, b->buf_bytes, &b->d_buf);
+    if (rc == IVR_OK) rc = dev_alloc(c, sizeof(unsigned long long), (void **) &b->d_ticket);
+    if (rc == IVR_OK && cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess) rc = IVR_ERR_CUDA;
+    if (rc) {
+        ivr_batch_free(b);
+        return rc;
+    }
+    *out = b;
+    return IVR_OK;
+}
+
+int ivr_batch_free(ivr_batch *b)
+{
+    if (!b) return IVR_ERR_INVALID;
+    batch_wait(b);
+    for (auto &g : b->graph)
+        if (g) cudaGraphExecDestroy(g);
+    if (b->done) cudaEventDestroy(b->done);
+    dev_free(b->ctx, b->d_buf, b->buf_bytes);
+    dev_free(b->ctx, b->d_ticket, sizeof(unsigned long long));
+    if (b->h_buf) cudaFreeHost(b->h_buf);
+    delete b;
+    return IVR_OK;
+}
+
+int ivr_batch_clear(ivr_batch *b)
+{
+    if (!b) return IVR_ERR_INVALID;
+    int rc = batch_wait(b);
+    if (rc) return rc;
+    b->n = 0;
+    b->dtype = -1;
+    return IVR_OK;
+}
+
+int ivr_batch_add(ivr_batch *b, ivr_view *view, ivr_tf *tf, float *rgba32_dev, uint8_t *rgba8_dev)
+{
+    if (!b) return IVR_ERR_INVALID;
+    ivr_ctx *c = b->ctx;
+    if (!view || view->ctx != c) return fail(c, IVR_ERR_INVALID, "view missing or from another context");
+    if (!view->valid) return fail(c, IVR_ERR_INVALID, "ivr_set_view has not succeeded on this view");
+    if (view->p.preset != IVR_PRESET_CONFIG) return fail(c, IVR_ERR_UNSUPPORTED, "batches render the CONFIG preset");
+    if (b->n == b->cap) return fail(c, IVR_ERR_INVALID, "batch is full (%d frames)", b->cap);
+    if (b->dtype >= 0 && view->vol->dtype != b->dtype)
+        return fail(c, IVR_ERR_INVALID, "one batch renders volumes of one dtype");
+    int rc = batch_wait(b);
+    if (rc) return rc;
+    BatchItem &it = batch_items(b)[b->n];
+    // the frame descriptor; a TF new to the volume has its distance field
+    // built here, and finished before the batch can be launched on any
+    // stream
+    bool built = false;
+    rc = frame_for(view, tf, 0, 0, view->info.vw, view->info.vh, -1, 0, it.f, &built);
+    if (rc) return rc;
+    if (built) CK(c, cudaStreamSynchronize(0));
+    it.out32 = (float4 *) rgba32_dev;
+    it.out8 = (uchar4 *) rgba8_dev;
+    b->dtype = view->vol->dtype;
+    b->n++;
+    return IVR_OK;
+}
+
+int ivr_batch_render(ivr_batch *b, int use_graph, void *stream)
+{
+    if (!b) return IVR_ERR_INVALID;
+    if (b->n == 0) return IVR_OK;
+    batch_layout(b);
+    int rc = batch_launch(b, (cudaStream_t) stream, use_graph != 0);
+    if (rc) return rc;
+    CK(b->ctx, cudaEventRecord(b->done, (cudaStream_t) stream));
+    b->pending = true;
+    return IVR_OK;
+}
+
+int ivr_batch_autotune(ivr_batch *b, void *stream, int *variant, float *ms_per_variant)
+{
+    if (!b) return IVR_ERR_INVALID;
+    ivr_ctx *c = b->ctx;
+    if (b->n == 0) return fail(c, IVR_ERR_INVALID, "autotune needs a filled batch");
+    cudaStream_t s = (cudaStream_t) stream;
+    cudaEvent_t e0, e1;
+    CK(c, cudaEventCreate(&e0));
+    CK(c, cudaEventCreate(&e1));
+    int best = 0;
+    float best_ms = 0.0f;
+    for (int v = 0; v < kBatchVariants; v++) {
+        b->variant = v;
+        int rc = batch_wait(b);
+        batch_layout(b);
+        if (rc == IVR_OK) rc = batch_launch(b, s, false);  // warm-up
+        if (rc == IVR_OK && cudaEventRecord(e0, s) != cudaSuccess) rc = IVR_ERR_CUDA;
+        for (int r = 0; r < 3 && rc == IVR_OK; r++) rc = batch_launch(b, s, false);
+        if (rc == IVR_OK && cudaEventRecord(e1, s) != cudaSuccess) rc = IVR_ERR_CUDA;
+        float ms = 0.0f;
+        if (rc == IVR_OK && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+            rc = IVR_ERR_CUDA;
+        if (rc) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return rc == IVR_ERR_CUDA ? fail(c, rc, "autotune timing failed") : rc;
+        }
+        ms /= 3.0f;
+        if (ms_per_variant) ms_per_variant[v] = ms;
+        if (v == 0 || ms < best_ms) {
+            best = v;
+            best_ms = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->variant = best;
+    if (variant) *variant = best;
+    return IVR_OK;
+}
+
+int ivr_batch_set_variant(ivr_batch *b, int variant)
+{
+    if (!b) return IVR_ERR_INVALID;
+    if (variant < 0 || variant >= kBatchVariants) return fail(b->ctx, IVR_ERR_INVALID, "variant %d", variant);
+    b->variant = variant;
     return IVR_OK;
 }
 

@@ -65,6 +65,22 @@ struct FrameDesc {
 // kernel parameters are limited to 32764 bytes
 static_assert(sizeof(FrameDesc) <= 32000, "FrameDesc too large for a kernel parameter");
 
+// One frame of a batched launch (device copy).
+struct BatchItem {
+    float4 *out32;
+    uchar4 *out8;
+    long long tile0;   // first global tile number of this frame
+    int tiles_x;       // warp tiles per output row
+    int pad;
+    FrameDesc f;
+};
+struct BatchHeader {
+    int nitems;
+    int pad;
+    long long total_tiles;
+};
+constexpr int kBatchVariants = 6;  // warp tile 8x4 / 4x8 / 16x2, with and without PAIR
+
 // Host-side brick record (device array + geometry that does not depend on
 // the view).
 struct HostBrick {
@@ -77,7 +93,6 @@ struct HostBrick {
     void *data;         // device
     bool owns;          // false when it aliases the full volume
     float *mc_minmax;   // device [mcz][mcy][mcx][2]
-    uint8_t *empty;     // device [mcz][mcy][mcx]
     int mcx, mcy, mcz;
 };
 
@@ -108,5 +123,9 @@ cudaError_t noalloc_histogram(const void *data, int dtype, long long n, int hsiz
 // *tickets: how many tile tickets the launch takes from f.tickets (a
 // persistent CONFIG launch takes each tile once and each warp fails once).
 cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s, long long *tickets);
+// batched CONFIG frames of one volume dtype; *ticket must be zero at launch
+cudaError_t launch_batch(int dtype, int variant, const BatchHeader *hdr, const BatchItem *items,
+                         unsigned long long *ticket, cudaStream_t s);
+int batch_variant_tile_w(int variant);
 
 }  // namespace ivr

@@ -20,11 +20,15 @@ constexpr int kThreads = 128;
 #ifndef IVR_CFG_PAIR
 #define IVR_CFG_PAIR 1  // two CONFIG samples per loop iteration
 #endif
+constexpr bool kPair = IVR_CFG_PAIR != 0;
 #ifndef IVR_CFG_BLOCKS_PER_SM
 #define IVR_CFG_BLOCKS_PER_SM 8
 #endif
 // resident blocks per SM the CONFIG kernel is compiled for (8 = 64 registers)
 constexpr int kCfgBlocksPerSm = IVR_CFG_BLOCKS_PER_SM;
+// the batched kernel reads its frame from global memory and needs more
+// registers: 6 blocks (80 registers) per SM
+constexpr int kBatchBlocksPerSm = 6;
 
 template <int DT> struct VoxT;
 template <> struct VoxT<IVR_U8> { using T = uint8_t; };
@@ -302,7 +306,7 @@ __device__ __forceinline__ int cfg_first_ge(float t0, float dt, float idt, float
 // so it would have had zero opacity and left acc unchanged); an opaque cell's
 // samples are taken up to one past the exit without further checks.  Every
 // sample that is taken is computed exactly as without skipping.
-template <int DT, bool SKIP, bool CENSUS>
+template <int DT, bool SKIP, bool CENSUS, bool PAIR>
 __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float dy, float dz, float idx,
                           float idy, float idz, float t0, float dt, float idt, float4 &acc, bool &done,
                           unsigned long long &nexec, unsigned long long &nlat)
@@ -344,12 +348,11 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float
             }
             icheck = iexit + 1;
         }
-#if IVR_CFG_PAIR
-        // two samples per iteration: both samples' loads are in flight
+        // PAIR: two samples per iteration, both samples' loads in flight
         // before either is composited.  The second is only composited when
         // it comes before the next cell check and the first did not end the
         // ray; sample_cfg clamps its indices, so computing it is always safe.
-        if (!CENSUS) {
+        if (PAIR && !CENSUS) {
             const int lim = SKIP ? min(i1, icheck) : i1;
             const float t1 = cfg_t(t0, dt, i + 1);
             const float s0 = sample_cfg<DT>(b, x, y, z);
@@ -379,7 +382,6 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float
             }
             continue;
         }
-#endif
         const float s = sample_cfg<DT>(b, x, y, z);
         if (CENSUS) {
             nexec++;
@@ -465,7 +467,7 @@ __global__ void __launch_bounds__(kThreads) march_ref_kernel(const __grid_consta
 }
 
 // One CONFIG ray: pixel (i, j) of the viewport, all bricks front to back.
-template <int DT, bool SKIP, bool CENSUS>
+template <int DT, bool SKIP, bool CENSUS, bool PAIR>
 __device__ __forceinline__ float4 ray_cfg(const FrameDesc &f, int i, int j, unsigned long long &nexec,
                                           unsigned long long &nlat)
 {
@@ -492,9 +494,9 @@ __device__ __forceinline__ float4 ray_cfg(const FrameDesc &f, int i, int j, unsi
         const DevBrick &b = f.b[k];
         if (!in_rect(b, i, j)) continue;
         if (SKIP && b.empty != nullptr)
-            march_cfg<DT, true, CENSUS>(f, b, dx, dy, dz, idx, idy, idz, t0, dt, idt, acc, done, nexec, nlat);
+            march_cfg<DT, true, CENSUS, PAIR>(f, b, dx, dy, dz, idx, idy, idz, t0, dt, idt, acc, done, nexec, nlat);
         else
-            march_cfg<DT, false, CENSUS>(f, b, dx, dy, dz, idx, idy, idz, t0, dt, idt, acc, done, nexec, nlat);
+            march_cfg<DT, false, CENSUS, PAIR>(f, b, dx, dy, dz, idx, idy, idz, t0, dt, idt, acc, done, nexec, nlat);
     }
     return acc;
 }
@@ -507,14 +509,14 @@ __device__ __forceinline__ float4 ray_cfg(const FrameDesc &f, int i, int j, unsi
 #endif
 
 // One pixel of the output window (ow, oh) = (oj, oi).
-template <int DT, bool SKIP, bool CENSUS>
+template <int DT, bool SKIP, bool CENSUS, bool PAIR>
 __device__ __forceinline__ void pixel_cfg(const FrameDesc &f, int oi, int oj, float4 *out32, uchar4 *out8,
                                           unsigned long long &nexec, unsigned long long &nlat)
 {
     if (oj >= f.out_w || oi >= f.out_h) return;
     const int j = f.out_x + oj, i = f.out_y + oi;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (i < f.vh && j < f.vw) acc = ray_cfg<DT, SKIP, CENSUS>(f, i, j, nexec, nlat);
+    if (i < f.vh && j < f.vw) acc = ray_cfg<DT, SKIP, CENSUS, PAIR>(f, i, j, nexec, nlat);
     const long long o = (long long) oi * f.out_w + oj;
     if (out32) out32[o] = acc;
     if (out8) out8[o] = make_uchar4(q8(acc.x), q8(acc.y), q8(acc.z), q8(acc.w));
@@ -538,13 +540,13 @@ __global__ void __launch_bounds__(kThreads, kCfgBlocksPerSm) march_cfg_kernel(co
         if (lane == 0) ticket = atomicAdd(f.tickets, 1ull);
         const long long tile = (long long) (__shfl_sync(0xffffffffu, ticket, 0) - f.ticket_base);
         if (tile >= ntiles) break;
-        pixel_cfg<DT, SKIP, CENSUS>(f, (int) (tile / tiles_x) * 4 + (lane >> 3), (int) (tile % tiles_x) * 8 + (lane & 7),
-                                    out32, out8, nexec, nlat);
+        pixel_cfg<DT, SKIP, CENSUS, kPair>(f, (int) (tile / tiles_x) * 4 + (lane >> 3),
+                                           (int) (tile % tiles_x) * 8 + (lane & 7), out32, out8, nexec, nlat);
     }
 #else
     int i, j, oi, oj;
     pixel_of(f, i, j, oi, oj);
-    pixel_cfg<DT, SKIP, CENSUS>(f, oi, oj, out32, out8, nexec, nlat);
+    pixel_cfg<DT, SKIP, CENSUS, kPair>(f, oi, oj, out32, out8, nexec, nlat);
 #endif
     if (CENSUS) count_exec(f, nexec, nlat);
 }
@@ -597,7 +599,77 @@ cudaError_t launch_dt(const FrameDesc &f, float4 *o32, uchar4 *o8, cudaStream_t 
     return cudaGetLastError();
 }
 
+// Batched CONFIG kernel: the tiles of every frame of a batch in one
+// persistent launch.  Frame descriptors are in device memory (uploaded with
+// the batch); a warp's ticket is a global tile number, mapped to its frame by
+// a binary search over the frames' first tiles.  Warp tiles are TW x (32/TW)
+// pixels; PAIR takes two samples per loop iteration.
+template <int DT, int TW, bool PAIR>
+__global__ void __launch_bounds__(kThreads, kBatchBlocksPerSm)
+    march_batch_kernel(const BatchHeader *__restrict__ hdr, const BatchItem *__restrict__ items,
+                       unsigned long long *ticket)
+{
+    constexpr int TH = 32 / TW;
+    const int lane = threadIdx.x & 31;
+    const int n = hdr->nitems;
+    const long long total = hdr->total_tiles;
+    unsigned long long nexec = 0, nlat = 0;
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(ticket, 1ull);
+        const long long g = (long long) __shfl_sync(0xffffffffu, t, 0);
+        if (g >= total) break;
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (items[mid].tile0 <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        const BatchItem &it = items[lo];
+        const long long tile = g - it.tile0;
+        pixel_cfg<DT, true, false, PAIR>(it.f, (int) (tile / it.tiles_x) * TH + lane / TW,
+                                        (int) (tile % it.tiles_x) * TW + lane % TW, it.out32, it.out8, nexec, nlat);
+    }
+}
+
+template <int DT, int TW, bool PAIR>
+cudaError_t launch_batch_v(const BatchHeader *hdr, const BatchItem *items, unsigned long long *ticket,
+                           cudaStream_t s)
+{
+    auto kern = march_batch_kernel<DT, TW, PAIR>;
+    kern<<<persistent_grid(kern, 0), kThreads, 0, s>>>(hdr, items, ticket);
+    return cudaGetLastError();
+}
+
+template <int DT>
+cudaError_t launch_batch_dt(int variant, const BatchHeader *hdr, const BatchItem *items, unsigned long long *ticket,
+                            cudaStream_t s)
+{
+    switch (variant) {
+    case 0: return launch_batch_v<DT, 8, true>(hdr, items, ticket, s);
+    case 1: return launch_batch_v<DT, 8, false>(hdr, items, ticket, s);
+    case 2: return launch_batch_v<DT, 4, true>(hdr, items, ticket, s);
+    case 3: return launch_batch_v<DT, 4, false>(hdr, items, ticket, s);
+    case 4: return launch_batch_v<DT, 16, true>(hdr, items, ticket, s);
+    case 5: return launch_batch_v<DT, 16, false>(hdr, items, ticket, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 }  // namespace
+
+int batch_variant_tile_w(int variant) { return variant < 2 ? 8 : variant < 4 ? 4 : 16; }
+
+cudaError_t launch_batch(int dtype, int variant, const BatchHeader *hdr, const BatchItem *items,
+                         unsigned long long *ticket, cudaStream_t s)
+{
+    switch (dtype) {
+    case IVR_U8: return launch_batch_dt<IVR_U8>(variant, hdr, items, ticket, s);
+    case IVR_U16: return launch_batch_dt<IVR_U16>(variant, hdr, items, ticket, s);
+    case IVR_F32: return launch_batch_dt<IVR_F32>(variant, hdr, items, ticket, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
 
 cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s, long long *warps)
 {
