@@ -123,6 +123,11 @@ int ivr_destroy(ivr_ctx *ctx);
 const char *ivr_last_error(const ivr_ctx *ctx);
 int ivr_mem_used(const ivr_ctx *ctx, size_t *bytes);
 
+/* Device memory counted against the context's HBM budget (for callers'
+ * output buffers); free with the same size. */
+int ivr_device_alloc(ivr_ctx *ctx, size_t bytes, void **ptr);
+int ivr_device_free(ivr_ctx *ctx, void *ptr, size_t bytes);
+
 /* --- volume load / brick setup (readvoldata, readfromfile, initvolbbox) -- */
 /* Copies a host volume (x fastest, [d][h][w]) to the device.  byteswap != 0
  * reverses the bytes of every element (main.c:695-703 for f32). */
@@ -220,6 +225,58 @@ int ivr_batch_render(ivr_batch *batch, int use_graph, void *stream);
  * the timings. */
 int ivr_batch_autotune(ivr_batch *batch, void *stream, int *variant, float *ms_per_variant);
 int ivr_batch_set_variant(ivr_batch *batch, int variant);
+
+/* --- steering server: continuous batching over resident volumes ---------
+ * Replaces the ivrserver/relay frame path (main.c:206-250,
+ * myserver.c:133-165).  Clients submit requests at any time; a scheduler
+ * thread keeps `slots` batches in flight, each on its own stream with an
+ * output arena of arena_bytes taken from the context's HBM budget.  A free
+ * slot takes the queued requests that fit (one volume dtype, outputs within
+ * its arena) in arrival order and renders them in one batched launch (CONFIG
+ * preset); requests arriving meanwhile wait and are admitted as slots and
+ * arena memory free up.  Every frame equals ivr_render of the same view and
+ * TF.  While a server runs, its context is used by the server's threads:
+ * make no other calls on that context until ivr_server_destroy. */
+typedef struct ivr_server ivr_server;
+typedef struct ivr_server_config {
+    int slots;              /* batches in flight (streams), 1..16 */
+    int max_batch_frames;   /* frames per batch */
+    size_t arena_bytes;     /* RGBA8 output memory per slot; larger frames are rejected */
+    int poll_us;            /* scheduler wake-up interval when idle */
+    float step;             /* CONFIG sampling of every request */
+    float term_alpha;
+    int tilew, tileh;
+} ivr_server_config;
+typedef struct ivr_request {
+    int volume;               /* id from ivr_server_add_volume */
+    int tf;                   /* id from ivr_server_add_tf */
+    ivr_state state;          /* the steering STATE: view, window, opacity, clip */
+    uint8_t *rgba8_host;      /* viewport RGBA8, written before completion */
+    unsigned long long tag;   /* the caller's id, returned in the completion */
+} ivr_request;
+typedef struct ivr_completion {
+    unsigned long long tag;
+    int status;               /* IVR_OK, IVR_ERR_NOMEM (frame larger than an arena), ... */
+    int vw, vh;
+    double t_queue;           /* seconds from submit to the start of its batch */
+    double t_total;           /* seconds from submit to the frame in host memory */
+} ivr_completion;
+void ivr_server_config_default(ivr_server_config *cfg);
+int ivr_server_create(ivr_ctx *ctx, const ivr_server_config *cfg, ivr_server **out);
+int ivr_server_destroy(ivr_server *server);  /* finishes every queued request first */
+int ivr_server_add_volume(ivr_server *server, ivr_volume *vol, int dtype, int *id);
+/* registers a transfer function (copied; a TF edit is a new id) */
+int ivr_server_add_tf(ivr_server *server, const float *rgba, int n, int lut_offset, float lut_scale, int *id);
+int ivr_server_submit(ivr_server *server, const ivr_request *req);
+/* up to max completions, waiting up to wait_ms for the first */
+int ivr_server_poll(ivr_server *server, ivr_completion *out, int max, int *n, int wait_ms);
+int ivr_server_stats(ivr_server *server, long long *completed, long long *rejected, long long *batches, int *queued);
+/* Steering front end on 127.0.0.1:port (0 = any): per connection, a
+ * 184-byte STATE (finish, winwidth, winheight in network byte order,
+ * connection.c:167-200) is answered with the viewport's RGBA8 bytes
+ * (connection.c:203-215), rendering `volume` with `tf`; finish != 0 or a
+ * disconnect ends the connection. */
+int ivr_server_listen(ivr_server *server, int port, int volume, int tf, int *bound_port);
 
 /* --- compositing and output -------------------------------------------- */
 /* compositetiles (main.c:1203-1218): num sub-images of w*h RGBA floats in

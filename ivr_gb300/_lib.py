@@ -32,6 +32,40 @@ class RenderParams(ctypes.Structure):
     ]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("slots", ctypes.c_int),
+        ("max_batch_frames", ctypes.c_int),
+        ("arena_bytes", ctypes.c_size_t),
+        ("poll_us", ctypes.c_int),
+        ("step", ctypes.c_float),
+        ("term_alpha", ctypes.c_float),
+        ("tilew", ctypes.c_int),
+        ("tileh", ctypes.c_int),
+    ]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [
+        ("volume", ctypes.c_int),
+        ("tf", ctypes.c_int),
+        ("state", IvrState),
+        ("rgba8_host", ctypes.c_void_p),
+        ("tag", ctypes.c_ulonglong),
+    ]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [
+        ("tag", ctypes.c_ulonglong),
+        ("status", ctypes.c_int),
+        ("vw", ctypes.c_int),
+        ("vh", ctypes.c_int),
+        ("t_queue", ctypes.c_double),
+        ("t_total", ctypes.c_double),
+    ]
+
+
 class FrameInfo(ctypes.Structure):
     _fields_ = [
         ("vw", ctypes.c_int),
@@ -85,6 +119,18 @@ SIGNATURES = {
     "ivr_batch_render": (_I, [_P, _I, _P]),
     "ivr_batch_autotune": (_I, [_P, _P, ctypes.POINTER(_I), _PF]),
     "ivr_batch_set_variant": (_I, [_P, _I]),
+    "ivr_device_alloc": (_I, [_P, ctypes.c_size_t, ctypes.POINTER(_P)]),
+    "ivr_device_free": (_I, [_P, _P, ctypes.c_size_t]),
+    "ivr_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
+    "ivr_server_create": (_I, [_P, ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),
+    "ivr_server_destroy": (_I, [_P]),
+    "ivr_server_add_volume": (_I, [_P, _P, _I, ctypes.POINTER(_I)]),
+    "ivr_server_add_tf": (_I, [_P, _PF, _I, _I, _F, ctypes.POINTER(_I)]),
+    "ivr_server_submit": (_I, [_P, ctypes.POINTER(Request)]),
+    "ivr_server_poll": (_I, [_P, ctypes.POINTER(Completion), _I, ctypes.POINTER(_I), _I]),
+    "ivr_server_stats": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                              ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I)]),
+    "ivr_server_listen": (_I, [_P, _I, _I, _I, ctypes.POINTER(_I)]),
     "ivr_composite": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "ivr_quantize": (_I, [_P, _P, _P, ctypes.c_longlong, _P]),
 }

@@ -255,3 +255,76 @@ class Batch:
         if self.h:
             self.ctx.lib.ivr_batch_free(self.h)
             self.h = None
+
+
+class Server:
+    """The steering server (ivr_server_*): continuous batching over resident
+    volumes.  While it runs, its context belongs to the server's threads."""
+
+    def __init__(self, ctx: Context, slots=4, max_batch_frames=64, arena_mib=96, step=0.5, term_alpha=0.99,
+                 poll_us=100):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        cfg = _lib.ServerConfig()
+        self.lib.ivr_server_config_default(ctypes.byref(cfg))
+        cfg.slots, cfg.max_batch_frames = slots, max_batch_frames
+        cfg.arena_bytes = int(arena_mib) << 20
+        cfg.step, cfg.term_alpha, cfg.poll_us = step, term_alpha, poll_us
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        ctx.check(self.lib.ivr_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self.keep = {}  # tag -> host buffer, alive until completion
+
+    def add_volume(self, vol: Volume) -> int:
+        i = ctypes.c_int()
+        self.ctx.check(self.lib.ivr_server_add_volume(self.h, vol.h, vol.dtype, ctypes.byref(i)))
+        return i.value
+
+    def add_tf(self, rgba: np.ndarray, offset: int = 0, scale: float = 1.0) -> int:
+        lut = np.ascontiguousarray(rgba, dtype=np.float32).reshape(-1, 4)
+        i = ctypes.c_int()
+        self.ctx.check(self.lib.ivr_server_add_tf(self.h, lut.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                  len(lut), offset, scale, ctypes.byref(i)))
+        return i.value
+
+    def submit(self, volume: int, tf: int, state: IvrState, tag: int, out: np.ndarray = None) -> np.ndarray:
+        vw = (state.winwidth // self.cfg.tilew) * self.cfg.tilew
+        vh = (state.winheight // self.cfg.tileh) * self.cfg.tileh
+        if out is None:
+            out = np.empty((vh, vw, 4), np.uint8)
+        r = _lib.Request()
+        r.volume, r.tf, r.state, r.tag = volume, tf, state, tag
+        r.rgba8_host = out.ctypes.data
+        self.keep[tag] = out
+        self.ctx.check(self.lib.ivr_server_submit(self.h, ctypes.byref(r)))
+        return out
+
+    def poll(self, max_n: int = 256, wait_ms: int = 10):
+        buf = (_lib.Completion * max_n)()
+        n = ctypes.c_int()
+        self.ctx.check(self.lib.ivr_server_poll(self.h, buf, max_n, ctypes.byref(n), wait_ms))
+        res = []
+        for k in range(n.value):
+            c = buf[k]
+            out = self.keep.pop(c.tag, None)
+            res.append({"tag": c.tag, "status": c.status, "vw": c.vw, "vh": c.vh, "t_queue": c.t_queue,
+                        "t_total": c.t_total, "frame": out})
+        return res
+
+    def stats(self) -> dict:
+        c, r, b = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        q = ctypes.c_int()
+        self.ctx.check(self.lib.ivr_server_stats(self.h, ctypes.byref(c), ctypes.byref(r), ctypes.byref(b),
+                                                 ctypes.byref(q)))
+        return {"completed": c.value, "rejected": r.value, "batches": b.value, "queued": q.value}
+
+    def listen(self, volume: int, tf: int, port: int = 0) -> int:
+        p = ctypes.c_int()
+        self.ctx.check(self.lib.ivr_server_listen(self.h, port, volume, tf, ctypes.byref(p)))
+        return p.value
+
+    def close(self):
+        if self.h:
+            self.lib.ivr_server_destroy(self.h)
+            self.h = None

@@ -23,6 +23,7 @@ struct ivr_ctx {
     uchar4 *d_frame8 = nullptr;  // ivr_render_host staging
     size_t frame8_bytes = 0;
     unsigned tf_serial = 0;
+    unsigned long long grid_clock = 0;  // recency of the per-TF distance fields
 };
 
 struct ivr_volume {
@@ -39,13 +40,13 @@ struct ivr_volume {
     struct TfGrid {
         unsigned serial;
         int zero_alpha;
-        unsigned long long last_use;
+        unsigned long long last_use;  // ctx grid_clock
         std::vector<uint8_t *> dist;  // per brick
+        cudaEvent_t ev;               // after the last launch that read it
     };
-    std::vector<TfGrid> grids;
-    unsigned long long use_clock = 0;
+    std::vector<TfGrid *> grids;
 };
-constexpr size_t kMaxTfGrids = 16;
+constexpr size_t kMaxTfGrids = 128;
 
 struct ivr_tf {
     ivr_ctx *ctx = nullptr;
@@ -83,6 +84,8 @@ struct ivr_batch {
     bool pending = false;
     cudaGraphExec_t graph[ivr::kBatchVariants] = {};
     cudaStream_t graph_stream[ivr::kBatchVariants] = {};
+    std::vector<ivr_volume::TfGrid *> grids;  // read by the frames in the batch
+    unsigned long long clock0 = 0;           // grid_clock when it was cleared
 };
 
 namespace {
@@ -145,8 +148,12 @@ size_t mc_cells(const HostBrick &b) { return (size_t) b.mcx * b.mcy * b.mcz; }
 
 void free_grids(ivr_volume *v)
 {
-    for (auto &g : v->grids)
-        for (size_t k = 0; k < g.dist.size(); k++) dev_free(v->ctx, g.dist[k], mc_cells(v->bricks[k]));
+    if (!v->grids.empty()) cudaDeviceSynchronize();
+    for (auto *g : v->grids) {
+        for (size_t k = 0; k < g->dist.size(); k++) dev_free(v->ctx, g->dist[k], mc_cells(v->bricks[k]));
+        if (g->ev) cudaEventDestroy(g->ev);
+        delete g;
+    }
     v->grids.clear();
 }
 
@@ -224,37 +231,41 @@ int valid_params(ivr_ctx *c, const ivr_render_params *p)
 
 // The per-brick distance fields of the volume for a TF, built on `s` when
 // the TF (or a zero opacity scale) is new to the volume.  Up to kMaxTfGrids
-// are kept; the least recently used is rebuilt in place, after the device
-// has finished every launch that may still read it.
-int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s, const std::vector<uint8_t *> **out,
-            bool *built = nullptr)
+// are kept; beyond that the least recently used one not read by frames since
+// `protect_from` is rebuilt in place once the last launch that read it has
+// finished (its event), or a new one is added when every grid is protected.
+int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s, unsigned long long protect_from,
+            ivr_volume::TfGrid **out, bool *built = nullptr)
 {
     if (built) *built = false;
     ivr_ctx *c = v->ctx;
-    const unsigned long long now = ++v->use_clock;
-    for (auto &g : v->grids)
-        if (g.serial == tf->serial && g.zero_alpha == (int) zero_alpha) {
-            g.last_use = now;
-            *out = &g.dist;
+    const unsigned long long now = ++c->grid_clock;
+    for (auto *g : v->grids)
+        if (g->serial == tf->serial && g->zero_alpha == (int) zero_alpha) {
+            g->last_use = now;
+            *out = g;
             return IVR_OK;
         }
     ivr_volume::TfGrid *g = nullptr;
-    if (v->grids.size() < kMaxTfGrids) {
-        v->grids.push_back(ivr_volume::TfGrid{0, 0, 0, std::vector<uint8_t *>(v->bricks.size(), nullptr)});
-        g = &v->grids.back();
-        for (size_t k = 0; k < v->bricks.size(); k++) {
-            int rc = dev_alloc(c, mc_cells(v->bricks[k]), (void **) &g->dist[k]);
-            if (rc) {
-                for (size_t j = 0; j < k; j++) dev_free(c, g->dist[j], mc_cells(v->bricks[j]));
-                v->grids.pop_back();
-                return rc;
-            }
-        }
+    if (v->grids.size() >= kMaxTfGrids)
+        for (auto *h : v->grids)
+            if (h->last_use < protect_from && (!g || h->last_use < g->last_use)) g = h;
+    if (g) {
+        CK(c, cudaEventSynchronize(g->ev));
     } else {
-        g = &v->grids[0];
-        for (auto &h : v->grids)
-            if (h.last_use < g->last_use) g = &h;
-        CK(c, cudaDeviceSynchronize());
+        g = new ivr_volume::TfGrid{0, 0, 0, std::vector<uint8_t *>(v->bricks.size(), nullptr), nullptr};
+        int rc = IVR_OK;
+        if (cudaEventCreateWithFlags(&g->ev, cudaEventDisableTiming) != cudaSuccess) rc = IVR_ERR_CUDA;
+        for (size_t k = 0; k < v->bricks.size() && rc == IVR_OK; k++)
+            rc = dev_alloc(c, mc_cells(v->bricks[k]), (void **) &g->dist[k]);
+        if (rc) {
+            for (size_t k = 0; k < v->bricks.size(); k++)
+                if (g->dist[k]) dev_free(c, g->dist[k], mc_cells(v->bricks[k]));
+            if (g->ev) cudaEventDestroy(g->ev);
+            delete g;
+            return rc == IVR_ERR_CUDA ? fail(c, rc, "event for a distance field") : rc;
+        }
+        v->grids.push_back(g);
     }
     g->serial = tf->serial;
     g->zero_alpha = (int) zero_alpha;
@@ -265,7 +276,8 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s, co
         else CK(c, launch_empty_flags(b.mc_minmax, b.mcx, b.mcy, b.mcz, tf->d_nzprefix, tf->n, tf->off, tf->scale,
                                       g->dist[k], s));
     }
-    *out = &g->dist;
+    CK(c, cudaEventRecord(g->ev, s));
+    *out = g;
     if (built) *built = true;
     return IVR_OK;
 }
@@ -273,9 +285,10 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s, co
 // Fills everything of a launch's frame descriptor that depends on the TF,
 // the output window and the skipping grid.
 int frame_for(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single, cudaStream_t s, FrameDesc &f,
-              bool *built = nullptr)
+              ivr_volume::TfGrid **grid, unsigned long long protect_from = ~0ull, bool *built = nullptr)
 {
     if (built) *built = false;
+    *grid = nullptr;
     ivr_ctx *c = view->ctx;
     if (!view->valid) return fail(c, IVR_ERR_INVALID, "ivr_set_view has not succeeded on this view");
     if (!tf) return fail(c, IVR_ERR_INVALID, "null transfer function");
@@ -296,10 +309,9 @@ int frame_for(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single
     f.single = single;
     f.counters = nullptr;
     if (view->p.skip == IVR_SKIP_GRID && view->p.preset == IVR_PRESET_CONFIG) {
-        const std::vector<uint8_t *> *dist = nullptr;
-        int rc = tf_grid(view->vol, tf, !(f.alpha != 0.0f), s, &dist, built);
+        int rc = tf_grid(view->vol, tf, !(f.alpha != 0.0f), s, protect_from, grid, built);
         if (rc) return rc;
-        for (int k = 0; k < f.nb; k++) f.b[k].empty = (*dist)[k];
+        for (int k = 0; k < f.nb; k++) f.b[k].empty = (*grid)->dist[k];
     }
     return IVR_OK;
 }
@@ -311,7 +323,8 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
     if (!view) return fail(c, IVR_ERR_INVALID, "null view");
     cudaStream_t s = (cudaStream_t) stream;
     FrameDesc f;
-    int rc = frame_for(view, tf, x, y, w, h, single, s, f);
+    ivr_volume::TfGrid *grid = nullptr;
+    int rc = frame_for(view, tf, x, y, w, h, single, s, f, &grid, c->grid_clock + 1);
     if (rc) return rc;
     if (touched) f.counters = c->d_counters;  // census launches count
     if (touched) {
@@ -332,6 +345,7 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
         return cuda_fail(c, e, "march launch");
     }
     view->ticket_base += (unsigned long long) used;
+    if (grid) CK(c, cudaEventRecord(grid->ev, s));
     return IVR_OK;
 }
 
@@ -405,6 +419,20 @@ int ivr_mem_used(const ivr_ctx *c, size_t *bytes)
 {
     if (!c || !bytes) return IVR_ERR_INVALID;
     *bytes = c->used;
+    return IVR_OK;
+}
+
+int ivr_device_alloc(ivr_ctx *c, size_t bytes, void **ptr)
+{
+    if (!c || !ptr) return IVR_ERR_INVALID;
+    CK(c, cudaSetDevice(c->device));
+    return dev_alloc(c, bytes, ptr);
+}
+
+int ivr_device_free(ivr_ctx *c, void *ptr, size_t bytes)
+{
+    if (!c) return IVR_ERR_INVALID;
+    dev_free(c, ptr, bytes);
     return IVR_OK;
 }
 
@@ -858,6 +886,8 @@ int ivr_batch_clear(ivr_batch *b)
     if (rc) return rc;
     b->n = 0;
     b->dtype = -1;
+    b->grids.clear();
+    b->clock0 = b->ctx->grid_clock + 1;
     return IVR_OK;
 }
 
@@ -878,9 +908,12 @@ int ivr_batch_add(ivr_batch *b, ivr_view *view, ivr_tf *tf, float *rgba32_dev, u
     // built here, and finished before the batch can be launched on any
     // stream
     bool built = false;
-    rc = frame_for(view, tf, 0, 0, view->info.vw, view->info.vh, -1, 0, it.f, &built);
+    ivr_volume::TfGrid *grid = nullptr;
+    if (b->n == 0) b->clock0 = c->grid_clock + 1;
+    rc = frame_for(view, tf, 0, 0, view->info.vw, view->info.vh, -1, 0, it.f, &grid, b->clock0, &built);
     if (rc) return rc;
     if (built) CK(c, cudaStreamSynchronize(0));
+    if (grid) b->grids.push_back(grid);
     it.out32 = (float4 *) rgba32_dev;
     it.out8 = (uchar4 *) rgba8_dev;
     b->dtype = view->vol->dtype;
@@ -895,6 +928,7 @@ int ivr_batch_render(ivr_batch *b, int use_graph, void *stream)
     batch_layout(b);
     int rc = batch_launch(b, (cudaStream_t) stream, use_graph != 0);
     if (rc) return rc;
+    for (auto *g : b->grids) CK(b->ctx, cudaEventRecord(g->ev, (cudaStream_t) stream));
     CK(b->ctx, cudaEventRecord(b->done, (cudaStream_t) stream));
     b->pending = true;
     return IVR_OK;

@@ -1,0 +1,528 @@
+// ivr_server.cpp -- the steering server: continuous batching of render
+// requests over resident volumes.
+//
+// Replaces the reference's frame path of ivrserver + relay
+// (main.c:206-250, myserver.c:133-165): instead of one client whose STATE is
+// broadcast to MPI ranks and answered with one frame, many clients submit
+// requests (a resident volume, a STATE, a transfer function, an RGBA8 output
+// buffer) at any time.  A scheduler thread keeps several batch slots in
+// flight, each on its own stream with its own device output arena: whenever a
+// slot is free it takes the queued requests that fit (same volume dtype,
+// output bytes within the arena -- the HBM admission rule), renders them in one
+// persistent batched launch, copies the RGBA8 frames back and records
+// completion times.  Requests that arrive while slots are busy wait in the
+// queue and are admitted as slots and arena memory free up, so batches
+// overlap on the device.
+//
+// The optional TCP front end speaks the reference's steering protocol: a
+// client sends the 184-byte STATE (finish, winwidth, winheight in network
+// byte order, connection.c:167-200) and receives the viewport as RGBA8
+// (connection.c:203-215).
+#include <arpa/inet.h>
+#include <netinet/in.h>
+#include <netinet/tcp.h>
+#include <sys/socket.h>
+#include <unistd.h>
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <future>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ivr_gpu.h"
+
+namespace {
+
+double now_s()
+{
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Req {
+    ivr_request r;
+    double t_submit;
+    int vw, vh;
+    size_t bytes;
+    std::shared_ptr<std::promise<int>> notify;  // front-end requests
+    ivr_completion c;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    void *arena = nullptr;   // device RGBA8 outputs of one batch
+    void *pinned = nullptr;  // host staging of the same size
+    std::vector<ivr_view *> views;
+    ivr_batch *batch[3] = {nullptr, nullptr, nullptr};  // per dtype
+    cudaEvent_t ev = nullptr;
+    bool busy = false;
+    std::vector<Req> reqs;
+    std::vector<size_t> offs;
+    double t_start = 0.0;
+};
+
+struct PendingTf {
+    int id;
+    std::vector<float> lut;
+    int n, off;
+    float scale;
+};
+
+}  // namespace
+
+struct ivr_server {
+    ivr_ctx *ctx = nullptr;
+    int device = 0;
+    ivr_server_config cfg{};
+    ivr_render_params params{};
+    std::vector<ivr_volume *> vols;
+    std::vector<int> vol_dtype;
+    std::vector<ivr_tf *> tfs;  // materialised on the scheduler thread
+    std::deque<PendingTf> pending_tfs;
+    int next_tf = 0;
+    std::deque<Req> queue;
+    std::deque<ivr_completion> done;
+    std::vector<Slot> slots;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::thread sched;
+    bool stop = false;
+    std::atomic<long long> completed{0}, rejected{0}, batches{0};
+    double busy_frames = 0;
+    // TCP front end
+    int listen_fd = -1;
+    std::thread acceptor;
+    std::vector<std::thread> conns;
+    std::atomic<bool> net_stop{false};
+    int net_tf = 0;
+    int net_volume = 0;
+    std::atomic<unsigned long long> net_tag{1ull << 62};
+    std::string err;
+};
+
+namespace {
+
+int viewport_dim(int win, int tile) { return (win / tile) * tile; }
+
+void complete(ivr_server *s, Req &q, int status, double t_start)
+{
+    q.c.tag = q.r.tag;
+    q.c.status = status;
+    q.c.vw = q.vw;
+    q.c.vh = q.vh;
+    q.c.t_queue = t_start > 0.0 ? t_start - q.t_submit : 0.0;
+    q.c.t_total = now_s() - q.t_submit;
+    if (status == IVR_OK) s->completed++;
+    else s->rejected++;
+    if (q.notify) {
+        q.notify->set_value(status);
+        return;
+    }
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->done.push_back(q.c);
+    s->cv_done.notify_all();
+}
+
+// copies a finished slot's frames out and frees the slot
+void finish_slot(ivr_server *s, Slot &sl)
+{
+    for (size_t i = 0; i < sl.reqs.size(); i++) {
+        Req &q = sl.reqs[i];
+        memcpy(q.r.rgba8_host, (char *) sl.pinned + sl.offs[i], q.bytes);
+        complete(s, q, IVR_OK, sl.t_start);
+    }
+    sl.reqs.clear();
+    sl.offs.clear();
+    sl.busy = false;
+}
+
+void materialise_tfs(ivr_server *s)
+{
+    std::deque<PendingTf> todo;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        todo.swap(s->pending_tfs);
+    }
+    for (auto &p : todo) {
+        ivr_tf *tf = nullptr;
+        int rc = ivr_tf_create(s->ctx, &tf);
+        if (rc == IVR_OK) rc = ivr_tf_set_lut(tf, p.lut.data(), p.n, p.off, p.scale, IVR_TF_F2B);
+        if ((int) s->tfs.size() <= p.id) s->tfs.resize(p.id + 1, nullptr);
+        s->tfs[p.id] = rc == IVR_OK ? tf : nullptr;
+        if (rc != IVR_OK && tf) ivr_tf_free(tf);
+    }
+}
+
+// takes the queued requests that fit a free slot and launches them
+bool dispatch(ivr_server *s, Slot &sl)
+{
+    std::vector<Req> take, never;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        if (s->queue.empty()) return false;
+        const int dtype = s->vol_dtype[s->queue.front().r.volume];
+        size_t used = 0;
+        for (auto it = s->queue.begin(); it != s->queue.end() && (int) take.size() < s->cfg.max_batch_frames;) {
+            if (it->bytes > s->cfg.arena_bytes) {  // larger than an arena: never admitted
+                never.push_back(*it);
+                it = s->queue.erase(it);
+                continue;
+            }
+            if (s->vol_dtype[it->r.volume] != dtype) {
+                ++it;
+                continue;
+            }
+            if (used + it->bytes > s->cfg.arena_bytes) break;  // arrival order: wait for the next slot
+            used += it->bytes;
+            take.push_back(*it);
+            it = s->queue.erase(it);
+        }
+    }
+    for (auto &q : never) complete(s, q, IVR_ERR_NOMEM, 0.0);
+    if (take.empty()) return !never.empty();
+    const int dtype = s->vol_dtype[take[0].r.volume];
+    ivr_batch *&b = sl.batch[dtype];
+    if (!b && ivr_batch_create(s->ctx, s->cfg.max_batch_frames, &b) != IVR_OK) b = nullptr;
+    sl.t_start = now_s();
+    size_t off = 0;
+    std::vector<Req> ok;
+    if (b) ivr_batch_clear(b);
+    for (auto &q : take) {
+        ivr_view *view = sl.views[ok.size()];
+        ivr_tf *tf = (q.r.tf >= 0 && q.r.tf < (int) s->tfs.size()) ? s->tfs[q.r.tf] : nullptr;
+        int rc = b ? IVR_OK : IVR_ERR_NOMEM;
+        if (rc == IVR_OK && !tf) rc = IVR_ERR_INVALID;
+        if (rc == IVR_OK) rc = ivr_set_view(view, s->vols[q.r.volume], &q.r.state, &s->params);
+        if (rc == IVR_OK) rc = ivr_batch_add(b, view, tf, nullptr, (uint8_t *) sl.arena + off);
+        if (rc != IVR_OK) {
+            complete(s, q, rc, sl.t_start);
+            continue;
+        }
+        sl.offs.push_back(off);
+        off += q.bytes;
+        ok.push_back(q);
+    }
+    if (ok.empty()) return true;
+    int rc = ivr_batch_render(b, 1, sl.stream);
+    if (rc == IVR_OK && cudaMemcpyAsync(sl.pinned, sl.arena, off, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
+        rc = IVR_ERR_CUDA;
+    if (rc == IVR_OK && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) rc = IVR_ERR_CUDA;
+    if (rc != IVR_OK) {
+        for (auto &q : ok) complete(s, q, rc, sl.t_start);
+        sl.offs.clear();
+        return true;
+    }
+    sl.reqs = std::move(ok);
+    sl.busy = true;
+    s->batches++;
+    return true;
+}
+
+void scheduler(ivr_server *s)
+{
+    cudaSetDevice(s->device);
+    for (;;) {
+        bool did = false;
+        for (auto &sl : s->slots)
+            if (sl.busy && cudaEventQuery(sl.ev) == cudaSuccess) {
+                finish_slot(s, sl);
+                did = true;
+            }
+        materialise_tfs(s);
+        for (auto &sl : s->slots)
+            if (!sl.busy) did |= dispatch(s, sl);
+        std::unique_lock<std::mutex> lock(s->mu);
+        if (s->stop) {
+            bool busy = false;
+            for (auto &sl : s->slots) busy |= sl.busy;
+            if (!busy && s->queue.empty()) break;
+        }
+        if (!did) s->cv_work.wait_for(lock, std::chrono::microseconds(s->cfg.poll_us));
+    }
+}
+
+int submit_req(ivr_server *s, const ivr_request *r, std::shared_ptr<std::promise<int>> notify)
+{
+    if (r->volume < 0 || r->volume >= (int) s->vols.size()) return IVR_ERR_INVALID;
+    if (!r->rgba8_host) return IVR_ERR_INVALID;
+    Req q;
+    q.r = *r;
+    q.t_submit = now_s();
+    q.vw = viewport_dim(r->state.winwidth, s->params.tilew);
+    q.vh = viewport_dim(r->state.winheight, s->params.tileh);
+    if (q.vw < 1 || q.vh < 1) return IVR_ERR_INVALID;
+    q.bytes = (size_t) q.vw * q.vh * 4;
+    q.notify = std::move(notify);
+    memset(&q.c, 0, sizeof(q.c));
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        if (s->stop) return IVR_ERR_INVALID;
+        s->queue.push_back(q);
+    }
+    s->cv_work.notify_one();
+    return IVR_OK;
+}
+
+bool recv_all(int fd, void *buf, size_t n)
+{
+    char *p = (char *) buf;
+    while (n > 0) {
+        ssize_t r = recv(fd, p, n, 0);
+        if (r <= 0) return false;
+        p += r;
+        n -= (size_t) r;
+    }
+    return true;
+}
+
+bool send_all(int fd, const void *buf, size_t n)
+{
+    const char *p = (const char *) buf;
+    while (n > 0) {
+        ssize_t r = send(fd, p, n, MSG_NOSIGNAL);
+        if (r <= 0) return false;
+        p += r;
+        n -= (size_t) r;
+    }
+    return true;
+}
+
+// one steering client: STATE in, frame out, until finish or disconnect
+void serve_conn(ivr_server *s, int fd)
+{
+    int one = 1;
+    setsockopt(fd, IPPROTO_TCP, TCP_NODELAY, &one, sizeof(one));
+    std::vector<uint8_t> frame;
+    for (;;) {
+        ivr_state st;
+        if (!recv_all(fd, &st, sizeof(st))) break;  // short read or disconnect
+        st.finish = (int) ntohl((uint32_t) st.finish);
+        st.winwidth = (int) ntohl((uint32_t) st.winwidth);
+        st.winheight = (int) ntohl((uint32_t) st.winheight);
+        if (st.finish) break;
+        ivr_request r;
+        memset(&r, 0, sizeof(r));
+        r.volume = s->net_volume;
+        r.tf = s->net_tf;
+        r.state = st;
+        r.tag = s->net_tag++;
+        const int vw = viewport_dim(st.winwidth, s->params.tilew), vh = viewport_dim(st.winheight, s->params.tileh);
+        if (vw < 1 || vh < 1 || (long long) vw * vh > (1LL << 26)) break;
+        frame.resize((size_t) vw * vh * 4);
+        r.rgba8_host = frame.data();
+        auto p = std::make_shared<std::promise<int>>();
+        auto fut = p->get_future();
+        if (submit_req(s, &r, p) != IVR_OK) break;
+        if (fut.get() != IVR_OK) break;
+        if (!send_all(fd, frame.data(), frame.size())) break;
+    }
+    close(fd);
+}
+
+void accept_loop(ivr_server *s)
+{
+    while (!s->net_stop) {
+        int fd = accept(s->listen_fd, nullptr, nullptr);
+        if (fd < 0) {
+            if (s->net_stop) break;
+            continue;
+        }
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->conns.emplace_back(serve_conn, s, fd);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void ivr_server_config_default(ivr_server_config *c)
+{
+    if (!c) return;
+    c->slots = 4;
+    c->max_batch_frames = 64;
+    c->arena_bytes = (size_t) 96 << 20;
+    c->poll_us = 100;
+    c->step = 0.5f;
+    c->term_alpha = 0.99f;
+    c->tilew = 1;
+    c->tileh = 1;
+}
+
+int ivr_server_create(ivr_ctx *ctx, const ivr_server_config *cfg, ivr_server **out)
+{
+    if (!ctx || !out) return IVR_ERR_INVALID;
+    *out = nullptr;
+    ivr_server_config c;
+    ivr_server_config_default(&c);
+    if (cfg) c = *cfg;
+    if (c.slots < 1 || c.slots > 16 || c.max_batch_frames < 1 || c.max_batch_frames > 1024 || c.arena_bytes < 4 ||
+        c.poll_us < 1)
+        return IVR_ERR_INVALID;
+    ivr_server *s = new ivr_server();
+    s->ctx = ctx;
+    s->cfg = c;
+    cudaGetDevice(&s->device);  // the context's device (current after ivr_create)
+    ivr_params_config(&s->params);
+    s->params.step = c.step;
+    s->params.term_alpha = c.term_alpha;
+    s->params.tilew = c.tilew;
+    s->params.tileh = c.tileh;
+    s->slots.resize(c.slots);
+    int rc = IVR_OK;
+    for (auto &sl : s->slots) {
+        // the output arenas come out of the context's HBM budget
+        if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaMallocHost(&sl.pinned, c.arena_bytes) != cudaSuccess) {
+            rc = IVR_ERR_CUDA;
+            break;
+        }
+        if ((rc = ivr_device_alloc(ctx, c.arena_bytes, &sl.arena)) != IVR_OK) break;
+        sl.views.resize(c.max_batch_frames, nullptr);
+        for (auto &v : sl.views)
+            if ((rc = ivr_view_create(ctx, &v)) != IVR_OK) break;
+        if (rc) break;
+    }
+    if (rc != IVR_OK) {
+        ivr_server_destroy(s);
+        return rc;
+    }
+    s->sched = std::thread(scheduler, s);
+    *out = s;
+    return IVR_OK;
+}
+
+int ivr_server_add_volume(ivr_server *s, ivr_volume *vol, int dtype, int *id)
+{
+    if (!s || !vol || !id || dtype < IVR_U8 || dtype > IVR_F32) return IVR_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (!s->queue.empty()) return IVR_ERR_INVALID;  // volumes are registered before serving
+    s->vols.push_back(vol);
+    s->vol_dtype.push_back(dtype);
+    *id = (int) s->vols.size() - 1;
+    return IVR_OK;
+}
+
+int ivr_server_add_tf(ivr_server *s, const float *rgba, int n, int lut_offset, float lut_scale, int *id)
+{
+    if (!s || !rgba || n < 1 || n > (1 << 24) || !id || !(lut_scale > 0.0f)) return IVR_ERR_INVALID;
+    PendingTf p;
+    p.lut.assign(rgba, rgba + 4 * (size_t) n);
+    p.n = n;
+    p.off = lut_offset;
+    p.scale = lut_scale;
+    std::lock_guard<std::mutex> lock(s->mu);
+    p.id = s->next_tf++;
+    *id = p.id;
+    s->pending_tfs.push_back(std::move(p));
+    s->cv_work.notify_one();
+    return IVR_OK;
+}
+
+int ivr_server_submit(ivr_server *s, const ivr_request *r)
+{
+    if (!s || !r) return IVR_ERR_INVALID;
+    return submit_req(s, r, nullptr);
+}
+
+int ivr_server_poll(ivr_server *s, ivr_completion *out, int max, int *n, int wait_ms)
+{
+    if (!s || !out || !n || max < 1) return IVR_ERR_INVALID;
+    std::unique_lock<std::mutex> lock(s->mu);
+    if (s->done.empty() && wait_ms > 0)
+        s->cv_done.wait_for(lock, std::chrono::milliseconds(wait_ms), [&] { return !s->done.empty(); });
+    int k = 0;
+    while (k < max && !s->done.empty()) {
+        out[k++] = s->done.front();
+        s->done.pop_front();
+    }
+    *n = k;
+    return IVR_OK;
+}
+
+int ivr_server_stats(ivr_server *s, long long *completed, long long *rejected, long long *batches, int *queued)
+{
+    if (!s) return IVR_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (completed) *completed = s->completed;
+    if (rejected) *rejected = s->rejected;
+    if (batches) *batches = s->batches;
+    if (queued) *queued = (int) s->queue.size();
+    return IVR_OK;
+}
+
+int ivr_server_listen(ivr_server *s, int port, int volume, int tf, int *bound_port)
+{
+    if (!s || s->listen_fd >= 0 || volume < 0 || volume >= (int) s->vols.size()) return IVR_ERR_INVALID;
+    int fd = socket(AF_INET, SOCK_STREAM, 0);
+    if (fd < 0) return IVR_ERR_IO;
+    int one = 1;
+    setsockopt(fd, SOL_SOCKET, SO_REUSEADDR, &one, sizeof(one));
+    sockaddr_in a;
+    memset(&a, 0, sizeof(a));
+    a.sin_family = AF_INET;
+    a.sin_addr.s_addr = htonl(INADDR_LOOPBACK);
+    a.sin_port = htons((uint16_t) port);
+    socklen_t len = sizeof(a);
+    if (bind(fd, (sockaddr *) &a, sizeof(a)) != 0 || listen(fd, 64) != 0 ||
+        getsockname(fd, (sockaddr *) &a, &len) != 0) {
+        close(fd);
+        return IVR_ERR_IO;
+    }
+    s->listen_fd = fd;
+    s->net_volume = volume;
+    s->net_tf = tf;
+    if (bound_port) *bound_port = ntohs(a.sin_port);
+    s->acceptor = std::thread(accept_loop, s);
+    return IVR_OK;
+}
+
+int ivr_server_destroy(ivr_server *s)
+{
+    if (!s) return IVR_ERR_INVALID;
+    if (s->listen_fd >= 0) {
+        s->net_stop = true;
+        shutdown(s->listen_fd, SHUT_RDWR);
+        close(s->listen_fd);
+        if (s->acceptor.joinable()) s->acceptor.join();
+    }
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->sched.joinable()) s->sched.join();
+    std::vector<std::thread> conns;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        conns.swap(s->conns);
+    }
+    for (auto &t : conns)
+        if (t.joinable()) t.join();
+    for (auto &sl : s->slots) {
+        for (auto *b : sl.batch)
+            if (b) ivr_batch_free(b);
+        for (auto *v : sl.views)
+            if (v) ivr_view_free(v);
+        if (sl.arena) ivr_device_free(s->ctx, sl.arena, s->cfg.arena_bytes);
+        if (sl.pinned) cudaFreeHost(sl.pinned);
+        if (sl.ev) cudaEventDestroy(sl.ev);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
+    for (auto *tf : s->tfs)
+        if (tf) ivr_tf_free(tf);
+    delete s;
+    return IVR_OK;
+}
+
+}  // extern "C"

@@ -37,6 +37,10 @@ def test_record_sizes():
     assert ctypes.sizeof(IvrState) == 184
     assert ctypes.sizeof(RenderParams) == 32
     assert ctypes.sizeof(FrameInfo) == 12 + 64 * 4 + 64 * 24 + 64 * 16
+    from ivr_gb300._lib import Completion, Request, ServerConfig
+    assert ctypes.sizeof(Request) == 4 + 4 + 184 + 8 + 8
+    assert ctypes.sizeof(Completion) == 8 + 4 * 3 + 4 + 16
+    assert ctypes.sizeof(ServerConfig) == 4 + 4 + 8 + 4 + 4 + 4 + 4 + 4 + 4
 
 
 def test_errors_without_device(gpu_lib):
