@@ -54,6 +54,12 @@ WORKLOADS = {
 # the autotuner
 BATCH = dict(base="sorted_brick_512", views=64, tfs=4, sizes=[(256, 256), (512, 512), (1024, 1024), (1920, 1080)],
              steps=(0.25, 1.0), seed=40)
+# steering-server workload: 4 resident volumes, 32 Poisson clients at 10-60
+# requests/s, a TF edit every 5th request, sizes 256^2 .. 1920x1080
+SERVE = dict(volumes=[((256, 256, 256), "u8", 8, 0.05, 0.0, 0.0), ((512, 512, 512), "u16", 64, 0.0, 0.0, 0.0),
+                      ((512, 512, 512), "f32", 64, 0.0, 0.1, 0.0), ((1024, 1024, 1024), "u16", 256, 0.0, 0.0, 0.7)],
+             clients=32, rate=(10.0, 60.0), duration=10.0, warm=2.0, slots=4, batch=16, arena_mib=160,
+             budget_gib=12)
 METRIC = "frames/s & Gsamples/s, learned-skip vs plain GPU at <=1/255 err; p99 ms"
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "march_cfg_sorted_brick_512.txt")
 
@@ -294,19 +300,74 @@ def run_batch(args):
     ctx.close()
 
 
+def run_serve(args):
+    """configs[4]: the steering server under Poisson load."""
+    import torch
+    from ivr_gb300 import api, serve, synth
+    torch.cuda.set_device(0)
+    ctx = api.Context(0, hbm_budget=SERVE["budget_gib"] << 30)
+    vols, scales, names = [], [], []
+    for k, (shape, dt, nb, noise, vn, zf) in enumerate(SERVE["volumes"]):
+        vol = synth.blob_volume(shape, n_blobs=nb, seed=50 + k, dtype=dt, noise=noise, value_noise=vn,
+                                zero_fraction=zf, device="cuda:0")
+        torch.cuda.empty_cache()
+        vols.append(ctx.load_volume(vol))
+        del vol
+        scales.append(256.0 / 65536.0 if dt == "u16" else 1.0)
+        names.append("x".join(map(str, shape)) + " " + dt)
+    resident = ctx.mem_used
+    srv = api.Server(ctx, slots=SERVE["slots"], max_batch_frames=SERVE["batch"], arena_mib=SERVE["arena_mib"])
+    ids = [srv.add_volume(v) for v in vols]
+    serve.run(srv, ids, scales, duration=SERVE["warm"], clients=SERVE["clients"], rate=SERVE["rate"], seed=1)
+    with ClockSampler(0) as clk:
+        res, wall = serve.run(srv, ids, scales, duration=SERVE["duration"], clients=SERVE["clients"],
+                              rate=SERVE["rate"], seed=2)
+    stats = srv.stats()
+    srv.close()
+    ok = [r for r in res if r["status"] == 0]
+    lat = np.array([r["latency"] for r in ok]) * 1000.0
+    px = sum(r["vw"] * r["vh"] for r in ok)
+    line = {
+        "metric": METRIC, "value": len(ok) / wall, "unit": "frames/s", "n_gpus": 1,
+        "steps": len(res), "warmup": 0, "ms_per_step": 1000.0 * wall / max(len(res), 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u16/f32",
+        "data": "synthetic (seeded blobs; Poisson arrivals)",
+        "config": {"workload": "serve_32", "volumes": names, "clients": SERVE["clients"],
+                   "rate_per_client": SERVE["rate"], "duration_s": SERVE["duration"],
+                   "sizes": "uniform from 256^2, 512^2, 1024^2, 1280x720, 1920x1080",
+                   "tf_edit": "every 5th request per client", "slots": SERVE["slots"],
+                   "max_batch_frames": SERVE["batch"], "arena_mib": SERVE["arena_mib"],
+                   "hbm_budget_gib": SERVE["budget_gib"], "resident_volume_bytes": resident},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "max": float(lat.max()), "from": "scheduled arrival to RGBA8 frame in host memory"},
+        "requests": len(res), "rejected": len(res) - len(ok),
+        "rejected_status": sorted({r["status"] for r in res if r["status"] != 0}),
+        "megapixels_per_s": px / wall / 1e6, "batches": stats["batches"],
+        "server_seconds": {k: stats[k] for k in ("gpu_s", "dispatch_s", "finish_s")}, "wall_s": wall,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    for v in vols:
+        v.free()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sorted_brick_512", choices=sorted(WORKLOADS) + ["batch_64x4"])
+    ap.add_argument("--workload", default="sorted_brick_512",
+                    choices=sorted(WORKLOADS) + ["batch_64x4", "serve_32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload == "batch_64x4":
         return run_batch(args)
+    if args.workload == "serve_32":
+        return run_serve(args)
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, wl)

@@ -246,6 +246,7 @@ typedef struct ivr_server_config {
     float step;             /* CONFIG sampling of every request */
     float term_alpha;
     int tilew, tileh;
+    int variant;            /* batch kernel variant (ivr_batch_set_variant) */
 } ivr_server_config;
 typedef struct ivr_request {
     int volume;               /* id from ivr_server_add_volume */
@@ -271,6 +272,9 @@ int ivr_server_submit(ivr_server *server, const ivr_request *req);
 /* up to max completions, waiting up to wait_ms for the first */
 int ivr_server_poll(ivr_server *server, ivr_completion *out, int max, int *n, int wait_ms);
 int ivr_server_stats(ivr_server *server, long long *completed, long long *rejected, long long *batches, int *queued);
+/* seconds: summed device time of the batches, and the scheduler's time
+ * forming/launching batches and copying frames out */
+int ivr_server_times(ivr_server *server, double *gpu_s, double *dispatch_s, double *finish_s);
 /* Steering front end on 127.0.0.1:port (0 = any): per connection, a
  * 184-byte STATE (finish, winwidth, winheight in network byte order,
  * connection.c:167-200) is answered with the viewport's RGBA8 bytes

@@ -42,6 +42,7 @@ class ServerConfig(ctypes.Structure):
         ("term_alpha", ctypes.c_float),
         ("tilew", ctypes.c_int),
         ("tileh", ctypes.c_int),
+        ("variant", ctypes.c_int),
     ]
 
 
@@ -131,6 +132,8 @@ SIGNATURES = {
     "ivr_server_stats": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                               ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I)]),
     "ivr_server_listen": (_I, [_P, _I, _I, _I, ctypes.POINTER(_I)]),
+    "ivr_server_times": (_I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_double)]),
     "ivr_composite": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "ivr_quantize": (_I, [_P, _P, _P, ctypes.c_longlong, _P]),
 }

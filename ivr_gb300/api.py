@@ -317,7 +317,10 @@ class Server:
         q = ctypes.c_int()
         self.ctx.check(self.lib.ivr_server_stats(self.h, ctypes.byref(c), ctypes.byref(r), ctypes.byref(b),
                                                  ctypes.byref(q)))
-        return {"completed": c.value, "rejected": r.value, "batches": b.value, "queued": q.value}
+        g, d, f = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self.ctx.check(self.lib.ivr_server_times(self.h, ctypes.byref(g), ctypes.byref(d), ctypes.byref(f)))
+        return {"completed": c.value, "rejected": r.value, "batches": b.value, "queued": q.value,
+                "gpu_s": g.value, "dispatch_s": d.value, "finish_s": f.value}
 
     def listen(self, volume: int, tf: int, port: int = 0) -> int:
         p = ctypes.c_int()

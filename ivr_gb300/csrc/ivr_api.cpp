@@ -43,6 +43,7 @@ struct ivr_volume {
         unsigned long long last_use;  // ctx grid_clock
         std::vector<uint8_t *> dist;  // per brick
         cudaEvent_t ev;               // after the last launch that read it
+        cudaEvent_t built;            // after its build
     };
     std::vector<TfGrid *> grids;
 };
@@ -152,6 +153,7 @@ void free_grids(ivr_volume *v)
     for (auto *g : v->grids) {
         for (size_t k = 0; k < g->dist.size(); k++) dev_free(v->ctx, g->dist[k], mc_cells(v->bricks[k]));
         if (g->ev) cudaEventDestroy(g->ev);
+        if (g->built) cudaEventDestroy(g->built);
         delete g;
     }
     v->grids.clear();
@@ -253,15 +255,18 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s, un
     if (g) {
         CK(c, cudaEventSynchronize(g->ev));
     } else {
-        g = new ivr_volume::TfGrid{0, 0, 0, std::vector<uint8_t *>(v->bricks.size(), nullptr), nullptr};
+        g = new ivr_volume::TfGrid{0, 0, 0, std::vector<uint8_t *>(v->bricks.size(), nullptr), nullptr, nullptr};
         int rc = IVR_OK;
-        if (cudaEventCreateWithFlags(&g->ev, cudaEventDisableTiming) != cudaSuccess) rc = IVR_ERR_CUDA;
+        if (cudaEventCreateWithFlags(&g->ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&g->built, cudaEventDisableTiming) != cudaSuccess)
+            rc = IVR_ERR_CUDA;
         for (size_t k = 0; k < v->bricks.size() && rc == IVR_OK; k++)
             rc = dev_alloc(c, mc_cells(v->bricks[k]), (void **) &g->dist[k]);
         if (rc) {
             for (size_t k = 0; k < v->bricks.size(); k++)
                 if (g->dist[k]) dev_free(c, g->dist[k], mc_cells(v->bricks[k]));
             if (g->ev) cudaEventDestroy(g->ev);
+            if (g->built) cudaEventDestroy(g->built);
             delete g;
             return rc == IVR_ERR_CUDA ? fail(c, rc, "event for a distance field") : rc;
         }
@@ -277,6 +282,7 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s, un
                                       g->dist[k], s));
     }
     CK(c, cudaEventRecord(g->ev, s));
+    CK(c, cudaEventRecord(g->built, s));
     *out = g;
     if (built) *built = true;
     return IVR_OK;
@@ -905,14 +911,14 @@ int ivr_batch_add(ivr_batch *b, ivr_view *view, ivr_tf *tf, float *rgba32_dev, u
     if (rc) return rc;
     BatchItem &it = batch_items(b)[b->n];
     // the frame descriptor; a TF new to the volume has its distance field
-    // built here, and finished before the batch can be launched on any
-    // stream
+    // built here on the legacy stream, and ivr_batch_render makes its stream
+    // wait for that build on the device
     bool built = false;
     ivr_volume::TfGrid *grid = nullptr;
     if (b->n == 0) b->clock0 = c->grid_clock + 1;
     rc = frame_for(view, tf, 0, 0, view->info.vw, view->info.vh, -1, 0, it.f, &grid, b->clock0, &built);
     if (rc) return rc;
-    if (built) CK(c, cudaStreamSynchronize(0));
+    (void) built;  // the render's stream waits for the build on the device
     if (grid) b->grids.push_back(grid);
     it.out32 = (float4 *) rgba32_dev;
     it.out8 = (uchar4 *) rgba8_dev;
@@ -926,6 +932,7 @@ int ivr_batch_render(ivr_batch *b, int use_graph, void *stream)
     if (!b) return IVR_ERR_INVALID;
     if (b->n == 0) return IVR_OK;
     batch_layout(b);
+    for (auto *g : b->grids) CK(b->ctx, cudaStreamWaitEvent((cudaStream_t) stream, g->built, 0));
     int rc = batch_launch(b, (cudaStream_t) stream, use_graph != 0);
     if (rc) return rc;
     for (auto *g : b->grids) CK(b->ctx, cudaEventRecord(g->ev, (cudaStream_t) stream));
@@ -940,6 +947,7 @@ int ivr_batch_autotune(ivr_batch *b, void *stream, int *variant, float *ms_per_v
     ivr_ctx *c = b->ctx;
     if (b->n == 0) return fail(c, IVR_ERR_INVALID, "autotune needs a filled batch");
     cudaStream_t s = (cudaStream_t) stream;
+    for (auto *g : b->grids) CK(c, cudaStreamWaitEvent(s, g->built, 0));
     cudaEvent_t e0, e1;
     CK(c, cudaEventCreate(&e0));
     CK(c, cudaEventCreate(&e1));

@@ -64,7 +64,9 @@ struct Slot {
     std::vector<ivr_view *> views;
     ivr_batch *batch[3] = {nullptr, nullptr, nullptr};  // per dtype
     cudaEvent_t ev = nullptr;
-    bool busy = false;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;  // timing of the batch's device work
+    bool busy = false;     // launched, or frames not yet copied out
+    bool copying = false;  // handed to the completion thread
     std::vector<Req> reqs;
     std::vector<size_t> offs;
     double t_start = 0.0;
@@ -94,10 +96,15 @@ struct ivr_server {
     std::vector<Slot> slots;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::thread sched;
+    std::thread sched, copier;
     bool stop = false;
+    std::deque<Slot *> to_copy;  // finished slots for the completion thread
+    std::condition_variable cv_copy;
+    bool copier_stop = false;
     std::atomic<long long> completed{0}, rejected{0}, batches{0};
-    double busy_frames = 0;
+    double gpu_s = 0.0;       // summed device time of the batches
+    double dispatch_s = 0.0;  // scheduler time spent forming and launching batches
+    double finish_s = 0.0;    // scheduler time spent copying frames out
     // TCP front end
     int listen_fd = -1;
     std::thread acceptor;
@@ -135,6 +142,9 @@ void complete(ivr_server *s, Req &q, int status, double t_start)
 // copies a finished slot's frames out and frees the slot
 void finish_slot(ivr_server *s, Slot &sl)
 {
+    const double t = now_s();
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, sl.t0, sl.t1) == cudaSuccess) s->gpu_s += ms / 1000.0;
     for (size_t i = 0; i < sl.reqs.size(); i++) {
         Req &q = sl.reqs[i];
         memcpy(q.r.rgba8_host, (char *) sl.pinned + sl.offs[i], q.bytes);
@@ -142,7 +152,31 @@ void finish_slot(ivr_server *s, Slot &sl)
     }
     sl.reqs.clear();
     sl.offs.clear();
+    std::lock_guard<std::mutex> lock(s->mu);
     sl.busy = false;
+    s->finish_s += now_s() - t;
+}
+
+// completion thread: copies finished slots' frames to the callers' buffers
+// (the scheduler keeps launching meanwhile) and then frees the slot
+void copier(ivr_server *s)
+{
+    for (;;) {
+        Slot *sl = nullptr;
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv_copy.wait(lock, [&] { return s->copier_stop || !s->to_copy.empty(); });
+            if (s->to_copy.empty()) return;
+            sl = s->to_copy.front();
+            s->to_copy.pop_front();
+        }
+        finish_slot(s, *sl);
+        {
+            std::lock_guard<std::mutex> lock(s->mu);
+            sl->copying = false;
+        }
+        s->cv_work.notify_one();
+    }
 }
 
 void materialise_tfs(ivr_server *s)
@@ -191,11 +225,19 @@ bool dispatch(ivr_server *s, Slot &sl)
     if (take.empty()) return !never.empty();
     const int dtype = s->vol_dtype[take[0].r.volume];
     ivr_batch *&b = sl.batch[dtype];
-    if (!b && ivr_batch_create(s->ctx, s->cfg.max_batch_frames, &b) != IVR_OK) b = nullptr;
+    if (!b) {
+        if (ivr_batch_create(s->ctx, s->cfg.max_batch_frames, &b) != IVR_OK) b = nullptr;
+        else ivr_batch_set_variant(b, s->cfg.variant);
+    }
     sl.t_start = now_s();
     size_t off = 0;
     std::vector<Req> ok;
     if (b) ivr_batch_clear(b);
+    for (auto &q : take)
+        if (q.r.tf >= (int) s->tfs.size() || (q.r.tf >= 0 && !s->tfs[q.r.tf])) {
+            materialise_tfs(s);  // registered after the last pass
+            break;
+        }
     for (auto &q : take) {
         ivr_view *view = sl.views[ok.size()];
         ivr_tf *tf = (q.r.tf >= 0 && q.r.tf < (int) s->tfs.size()) ? s->tfs[q.r.tf] : nullptr;
@@ -212,7 +254,9 @@ bool dispatch(ivr_server *s, Slot &sl)
         ok.push_back(q);
     }
     if (ok.empty()) return true;
+    cudaEventRecord(sl.t0, sl.stream);
     int rc = ivr_batch_render(b, 1, sl.stream);
+    if (rc == IVR_OK) cudaEventRecord(sl.t1, sl.stream);
     if (rc == IVR_OK && cudaMemcpyAsync(sl.pinned, sl.arena, off, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
         rc = IVR_ERR_CUDA;
     if (rc == IVR_OK && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) rc = IVR_ERR_CUDA;
@@ -222,7 +266,10 @@ bool dispatch(ivr_server *s, Slot &sl)
         return true;
     }
     sl.reqs = std::move(ok);
-    sl.busy = true;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        sl.busy = true;
+    }
     s->batches++;
     return true;
 }
@@ -232,14 +279,38 @@ void scheduler(ivr_server *s)
     cudaSetDevice(s->device);
     for (;;) {
         bool did = false;
-        for (auto &sl : s->slots)
-            if (sl.busy && cudaEventQuery(sl.ev) == cudaSuccess) {
-                finish_slot(s, sl);
+        for (auto &sl : s->slots) {
+            bool hand = false;
+            {
+                std::lock_guard<std::mutex> lock(s->mu);
+                hand = sl.busy && !sl.copying && cudaEventQuery(sl.ev) == cudaSuccess;
+                if (hand) {
+                    sl.copying = true;
+                    s->to_copy.push_back(&sl);
+                }
+            }
+            if (hand) {
+                s->cv_copy.notify_one();
                 did = true;
             }
+        }
         materialise_tfs(s);
-        for (auto &sl : s->slots)
-            if (!sl.busy) did |= dispatch(s, sl);
+        for (auto &sl : s->slots) {
+            bool idle;
+            {
+                std::lock_guard<std::mutex> lock(s->mu);
+                idle = !sl.busy;
+            }
+            if (idle) {
+                const double t = now_s();
+                const bool d = dispatch(s, sl);
+                if (d) {
+                    std::lock_guard<std::mutex> lock(s->mu);
+                    s->dispatch_s += now_s() - t;
+                }
+                did |= d;
+            }
+        }
         std::unique_lock<std::mutex> lock(s->mu);
         if (s->stop) {
             bool busy = false;
@@ -356,6 +427,7 @@ void ivr_server_config_default(ivr_server_config *c)
     c->term_alpha = 0.99f;
     c->tilew = 1;
     c->tileh = 1;
+    c->variant = 1;  // 8x4 warp tiles, one sample per iteration
 }
 
 int ivr_server_create(ivr_ctx *ctx, const ivr_server_config *cfg, ivr_server **out)
@@ -383,6 +455,7 @@ int ivr_server_create(ivr_ctx *ctx, const ivr_server_config *cfg, ivr_server **o
         // the output arenas come out of the context's HBM budget
         if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreate(&sl.t0) != cudaSuccess || cudaEventCreate(&sl.t1) != cudaSuccess ||
             cudaMallocHost(&sl.pinned, c.arena_bytes) != cudaSuccess) {
             rc = IVR_ERR_CUDA;
             break;
@@ -398,6 +471,7 @@ int ivr_server_create(ivr_ctx *ctx, const ivr_server_config *cfg, ivr_server **o
         return rc;
     }
     s->sched = std::thread(scheduler, s);
+    s->copier = std::thread(copier, s);
     *out = s;
     return IVR_OK;
 }
@@ -461,6 +535,16 @@ int ivr_server_stats(ivr_server *s, long long *completed, long long *rejected, l
     return IVR_OK;
 }
 
+int ivr_server_times(ivr_server *s, double *gpu_s, double *dispatch_s, double *finish_s)
+{
+    if (!s) return IVR_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (gpu_s) *gpu_s = s->gpu_s;
+    if (dispatch_s) *dispatch_s = s->dispatch_s;
+    if (finish_s) *finish_s = s->finish_s;
+    return IVR_OK;
+}
+
 int ivr_server_listen(ivr_server *s, int port, int volume, int tf, int *bound_port)
 {
     if (!s || s->listen_fd >= 0 || volume < 0 || volume >= (int) s->vols.size()) return IVR_ERR_INVALID;
@@ -502,6 +586,12 @@ int ivr_server_destroy(ivr_server *s)
     }
     s->cv_work.notify_all();
     if (s->sched.joinable()) s->sched.join();
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->copier_stop = true;
+    }
+    s->cv_copy.notify_all();
+    if (s->copier.joinable()) s->copier.join();
     std::vector<std::thread> conns;
     {
         std::lock_guard<std::mutex> lock(s->mu);
@@ -517,6 +607,8 @@ int ivr_server_destroy(ivr_server *s)
         if (sl.arena) ivr_device_free(s->ctx, sl.arena, s->cfg.arena_bytes);
         if (sl.pinned) cudaFreeHost(sl.pinned);
         if (sl.ev) cudaEventDestroy(sl.ev);
+        if (sl.t0) cudaEventDestroy(sl.t0);
+        if (sl.t1) cudaEventDestroy(sl.t1);
         if (sl.stream) cudaStreamDestroy(sl.stream);
     }
     for (auto *tf : s->tfs)

@@ -40,7 +40,7 @@ def test_record_sizes():
     from ivr_gb300._lib import Completion, Request, ServerConfig
     assert ctypes.sizeof(Request) == 4 + 4 + 184 + 8 + 8
     assert ctypes.sizeof(Completion) == 8 + 4 * 3 + 4 + 16
-    assert ctypes.sizeof(ServerConfig) == 4 + 4 + 8 + 4 + 4 + 4 + 4 + 4 + 4
+    assert ctypes.sizeof(ServerConfig) == 40
 
 
 def test_errors_without_device(gpu_lib):
