@@ -60,6 +60,16 @@ SERVE = dict(volumes=[((256, 256, 256), "u8", 8, 0.05, 0.0, 0.0), ((512, 512, 51
                       ((512, 512, 512), "f32", 64, 0.0, 0.1, 0.0), ((1024, 1024, 1024), "u16", 256, 0.0, 0.0, 0.7)],
              clients=32, rate=(10.0, 60.0), duration=10.0, warm=2.0, slots=4, batch=16, arena_mib=160,
              budget_gib=12)
+# learned empty-space skipping: 1024^3 u16 of 256 blobs (sigmas scaled by
+# (8/256)^(1/3) so they do not sum to saturation) with 70% of the
+# macrocells exactly zero, 1920x1080, 50 random 16-knot TFs (the lowest
+# fifteenth of the range transparent); the predictor is trained on the exact
+# bounds of 8 of them (65^3 cells x 8 = 2.2M samples) and every TF is
+# rendered plain (no skipping), with the exact grid and with the learned grid
+LEARNED = dict(shape=(1024, 1024, 1024), dtype="u16", n_blobs=256, sigma_scale=(8 / 256) ** (1 / 3),
+               zero_fraction=0.7, image=(1920, 1080),
+               step=0.5, term=0.99, fovy=30.0, seed=3, tfs=50, train_tfs=8, epochs=30, batch_rows=8192, lr=2e-3,
+               wneg=4.0, slack=0.02, judge_stride=16, frames=3)
 METRIC = "frames/s & Gsamples/s, learned-skip vs plain GPU at <=1/255 err; p99 ms"
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "march_cfg_sorted_brick_512.txt")
 
@@ -309,7 +319,7 @@ def run_serve(args):
     vols, scales, names = [], [], []
     for k, (shape, dt, nb, noise, vn, zf) in enumerate(SERVE["volumes"]):
         vol = synth.blob_volume(shape, n_blobs=nb, seed=50 + k, dtype=dt, noise=noise, value_noise=vn,
-                                zero_fraction=zf, device="cuda:0")
+                                zero_fraction=zf, device="cuda:0", sigma_scale=min(1.0, (8 / nb) ** (1 / 3)))
         torch.cuda.empty_cache()
         vols.append(ctx.load_volume(vol))
         del vol
@@ -352,6 +362,124 @@ def run_serve(args):
     ctx.close()
 
 
+def run_learned(args, quiet=False):
+    """configs[2]: learned skipping against the plain march and the exact grid."""
+    import torch
+    from ivr_gb300 import api, synth
+    from ivr_gb300.state import orbit_state
+    L = LEARNED
+    torch.cuda.set_device(0)
+    vol = synth.blob_volume(L["shape"], n_blobs=L["n_blobs"], seed=L["seed"], dtype=L["dtype"], noise=0.0,
+                            zero_fraction=L["zero_fraction"], device="cuda:0", sigma_scale=L["sigma_scale"])
+    torch.cuda.empty_cache()
+    ctx = api.Context(0)
+    v = ctx.load_volume(vol)
+    del vol
+    scale = 256.0 / 65536.0
+    tfs = [ctx.transfer_function().set_lut(synth.knot_tf(1000 + t, zero_first=True)[0], 0, scale, api.TF_F2B)
+           for t in range(L["tfs"])]
+    w, h = L["image"]
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+
+    # training on the device: exact bounds of train_tfs TFs, Adam, calibration
+    mlp = ctx.mlp(L["seed"])
+    t0 = time.perf_counter()
+    n = 0
+    for tf in tfs[:L["train_tfs"]]:
+        n = mlp.add_samples(v, tf)
+    t_feat = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    losses = mlp.train(L["epochs"], batch_rows=L["batch_rows"], lr=L["lr"], wneg=L["wneg"])
+    t_train = time.perf_counter() - t0
+    margin, recall = mlp.calibrate(L["slack"])
+    v.set_mlp(mlp, margin, certify=True)
+
+    methods = {"plain": api.SKIP_NONE, "grid": api.SKIP_GRID, "learned": api.SKIP_LEARNED}
+    vw = {m: ctx.view() for m in methods}
+    rng = np.random.default_rng(L["seed"] + 77)
+    states = [orbit_state(float(rng.uniform(0, 360)), float(rng.uniform(-60, 60)), w, h, fovy=L["fovy"])
+              for _ in range(L["tfs"])]
+    outs = {m: torch.empty((h, w, 4), dtype=torch.uint8, device="cuda") for m in methods}
+    ms = {m: [] for m in methods}
+    first_ms = {m: [] for m in methods}
+    lattice, executed = 0, {m: 0 for m in methods}
+    worst = 0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        for t, (tf, st) in enumerate(zip(tfs, states)):
+            for m, skip in methods.items():
+                p = api.config_params(step=L["step"], term_alpha=L["term"], skip=skip,
+                                      judge_stride=L["judge_stride"])
+                view = vw[m].set(v, st, p)
+                # first frame of a new TF: includes building its grid
+                torch.cuda.synchronize()
+                ev0.record(stream)
+                view.render(tf, None, outs[m].data_ptr(), sp)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                first_ms[m].append(ev0.elapsed_time(ev1))
+                ev0.record(stream)
+                for _ in range(L["frames"]):
+                    view.render(tf, None, outs[m].data_ptr(), sp)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                ms[m].append(ev0.elapsed_time(ev1) / L["frames"])
+            d = (outs["learned"].int() - outs["plain"].int()).abs().max().item()
+            worst = max(worst, d)
+            if t < 10:  # census of a subset: lattice and executed samples
+                for m in methods:
+                    c = vw[m].census(tf, sp)
+                    executed[m] += c["executed"]
+                lattice += c["lattice"]
+    judge = vw["learned"].judge_stats()
+    tot = {m: sum(ms[m]) for m in methods}
+    fps = {m: L["tfs"] / (tot[m] / 1000.0) for m in methods}
+    held = slice(L["train_tfs"], None)
+    fps_held = {m: len(ms[m][held]) / (sum(ms[m][held]) / 1000.0) for m in methods}
+    lat_per_frame = lattice / 10
+    ls = v.learned_stats()
+    line = {
+        "metric": METRIC, "value": fps["learned"], "unit": "frames/s", "n_gpus": 1,
+        "steps": L["tfs"] * L["frames"], "warmup": L["tfs"], "ms_per_step": tot["learned"] / L["tfs"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
+        "data": "synthetic (seeded blobs, 70% zero macrocells, random 16-knot TFs)",
+        "config": {"workload": "learned_1024",
+                   "volume": "1024x1024x1024 u16 (2 GiB), one brick, 256 blobs, 70% zero macrocells",
+                   "image": f"{w}x{h}", "tfs": L["tfs"], "train_tfs": L["train_tfs"], "step_voxels": L["step"],
+                   "early_termination_alpha": L["term"], "judge": f"1 in {L['judge_stride']} tiles, tol 1/255",
+                   "l2": "inputs larger than L2 (2 GiB volume resident)"},
+        "fps": fps, "fps_held_out_tfs": fps_held,
+        "learned_grid": dict(ls, recall_of_exact=(ls["learned_transparent"] - ls["false_skips"]) /
+                             max(ls["exact_transparent"], 1),
+                             note="cells over the 50 learned grids; false skips kept opaque by certification"),
+        "speedup": {"learned_vs_plain": fps["learned"] / fps["plain"], "learned_vs_grid": fps["learned"] / fps["grid"],
+                    "grid_vs_plain": fps["grid"] / fps["plain"]},
+        "gsamples_per_s": {m: lat_per_frame * fps[m] / 1e9 for m in methods},
+        "executed_per_frame": {m: executed[m] / 10 for m in methods}, "lattice_per_frame": lat_per_frame,
+        "max_abs_diff_8bit_vs_plain": worst,
+        "first_frame_ms_median": {m: float(np.median(first_ms[m])) for m in methods},
+        "frame_ms_median": {m: float(np.median(ms[m])) for m in methods},
+        "judge": judge,
+        "training": {"samples": n, "epochs": L["epochs"], "batch_rows": L["batch_rows"],
+                     "loss_first": float(losses[0]), "loss_last": float(losses[-1]), "features_s": t_feat,
+                     "train_s": t_train, "margin": margin, "recall_of_transparent_cells": recall},
+        "gpu_launches": L["tfs"] * (L["frames"] + 1) * 4,
+        "clocks": clk.summary(),
+    }
+    for m in methods:
+        vw[m].free()
+    v.set_mlp(None)
+    mlp.free()
+    for tf in tfs:
+        tf.free()
+    v.free()
+    ctx.close()
+    if not quiet:
+        print(json.dumps(line), flush=True)
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -359,7 +487,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sorted_brick_512",
-                    choices=sorted(WORKLOADS) + ["batch_64x4", "serve_32"])
+                    choices=sorted(WORKLOADS) + ["batch_64x4", "serve_32", "learned_1024"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     args = ap.parse_args()
@@ -368,6 +496,8 @@ def main():
         return run_batch(args)
     if args.workload == "serve_32":
         return run_serve(args)
+    if args.workload == "learned_1024":
+        return run_learned(args)
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, wl)

@@ -85,7 +85,10 @@ typedef enum { IVR_CM_BASE = 0, IVR_CM_RAINBOW = 1, IVR_CM_MEDICAL = 2, IVR_CM_S
 
 typedef enum { IVR_PRESET_REF = 0, IVR_PRESET_CONFIG = 1 } ivr_preset;
 typedef enum { IVR_ORDER_CENTER = 0, IVR_ORDER_AXIS = 1 } ivr_order;
-typedef enum { IVR_SKIP_NONE = 0, IVR_SKIP_GRID = 1 } ivr_skip;
+/* IVR_SKIP_GRID: the exact macrocell grid (never changes the image).
+ * IVR_SKIP_LEARNED: the grid the volume's learned predictor gives
+ * (ivr_volume_set_mlp), every frame judged against the exact grid. */
+typedef enum { IVR_SKIP_NONE = 0, IVR_SKIP_GRID = 1, IVR_SKIP_LEARNED = 2 } ivr_skip;
 
 /* How a frame is sampled.
  * REF: the reference's sampling exactly (ray.c): ray-parameter step 0.001,
@@ -100,8 +103,10 @@ typedef struct ivr_render_params {
     int max_samples;   /* per ray and brick; 0 = unbounded */
     float term_alpha;  /* early termination threshold (> 1 disables) */
     int order;         /* ivr_order */
-    int skip;          /* ivr_skip: empty-space skipping (never changes the image) */
+    int skip;          /* ivr_skip */
     int tilew, tileh;  /* viewport rounded down to multiples (argv[11..12]) */
+    int judge_stride;  /* IVR_SKIP_LEARNED: judge 1 in judge_stride 8x4 tiles, rotating */
+    int judge_tol;     /* IVR_SKIP_LEARNED: largest 8-bit channel difference accepted */
 } ivr_render_params;
 
 /* Per-frame geometry ivr_set_view computed, for callers that composite or
@@ -281,6 +286,83 @@ int ivr_server_times(ivr_server *server, double *gpu_s, double *dispatch_s, doub
  * (connection.c:203-215), rendering `volume` with `tf`; finish != 0 or a
  * disconnect ends the connection. */
 int ivr_server_listen(ivr_server *server, int port, int volume, int tf, int *bound_port);
+
+/* --- learned empty-space skipping ---------------------------------------
+ * No counterpart in the reference, which samples every lattice point.  A
+ * small MLP predicts, per macrocell and transfer function, an upper bound on
+ * the cell's post-TF opacity, so the skipping grid of a new TF comes from
+ * one batched inference.
+ *   inputs (26, zero padded to 32, BF16): the cell's min and max normalised
+ *     to the volume's range, its 8-bin value histogram (fractions), and the
+ *     TF's 16 knots: the largest LUT opacity over each sixteenth of the
+ *     volume's value range;
+ *   network: 26 -> 64 -> 64 -> 1, ReLU, BF16 weights and activations, FP32
+ *     accumulation on the tensor cores;
+ *   target: the exact bound the plain grid uses, the largest LUT opacity
+ *     over the index range of the cell's values.  A cell whose bound is 0
+ *     costs only when y > -IVR_MLP_TRANSPARENT; otherwise the loss is
+ *     w * (y - target)^2 with w = wneg for y < target, 1 above;
+ *   grid: a cell is transparent when y + margin <= 0.
+ * A view with skip = IVR_SKIP_LEARNED renders with that grid and, in the
+ * same launch, marches a rotating 1/judge_stride of its 8x4 tiles again
+ * with the exact grid and compares: when some 8-bit channel differs by more
+ * than judge_tol, the frame is re-rendered with the exact grid by a launch
+ * gated on the verdict (the decision stays on the device) and the TF's
+ * learned grid is not used again. */
+typedef struct ivr_mlp ivr_mlp;
+#define IVR_MLP_PARAMS 6337       /* W1[32][64] (rows 26-31 zero), b1[64], W2[64][64], b2[64], w3[64], b3 */
+#define IVR_MLP_IN 32             /* feature row width (BF16) */
+#define IVR_MLP_TRANSPARENT 0.5f  /* training code of a zero bound: y <= -0.5 costs nothing */
+typedef struct ivr_judge_stats {
+    unsigned long long frames;       /* frames judged */
+    unsigned long long fallbacks;    /* judged frames above tolerance, re-rendered with the exact grid */
+    unsigned long long pixels;       /* pixels compared */
+    int worst;                       /* largest 8-bit difference seen */
+    int pad;
+    unsigned long long exact_frames; /* learned-skip frames rendered with the exact grid because a
+                                        judged frame had already found their learned grid wrong */
+} ivr_judge_stats;
+int ivr_mlp_create(ivr_ctx *ctx, unsigned long long seed, ivr_mlp **out);  /* He-initialised */
+int ivr_mlp_free(ivr_mlp *mlp);
+int ivr_mlp_get_params(const ivr_mlp *mlp, float *params);  /* IVR_MLP_PARAMS floats */
+int ivr_mlp_set_params(ivr_mlp *mlp, const float *params);
+/* the parameters as a small binary file (magic, count, little-endian floats) */
+int ivr_mlp_save(const ivr_mlp *mlp, const char *path);
+int ivr_mlp_load(ivr_mlp *mlp, const char *path);
+/* Features ([n][IVR_MLP_IN] BF16) and exact bounds ([n] floats, nullable) of
+ * every macrocell of every brick of vol (brick order, cells x fastest) for
+ * tf; n = cells, at most cap. */
+int ivr_mlp_features(ivr_mlp *mlp, ivr_volume *vol, ivr_tf *tf, uint16_t *x_dev, float *bound_dev, long long cap,
+                     long long *n, void *stream);
+int ivr_mlp_forward(ivr_mlp *mlp, const uint16_t *x_dev, long long n, float *y_dev, void *stream);
+/* Training loss over n rows and its gradient (grad_dev: IVR_MLP_PARAMS
+ * floats, loss_dev: one float; both overwritten). */
+int ivr_mlp_gradient(ivr_mlp *mlp, const uint16_t *x_dev, const float *bound_dev, long long n, float wneg,
+                     float *grad_dev, float *loss_dev, void *stream);
+/* The training set: every macrocell of vol under tf, appended. */
+int ivr_mlp_add_samples(ivr_mlp *mlp, ivr_volume *vol, ivr_tf *tf, long long *total);
+int ivr_mlp_clear_samples(ivr_mlp *mlp);
+/* Adam over shuffled mini-batches of batch_rows; loss_per_epoch (nullable)
+ * receives the mean batch loss of each epoch. */
+int ivr_mlp_train(ivr_mlp *mlp, int epochs, int batch_rows, float lr, float wneg, float *loss_per_epoch);
+/* The smallest margin with y + margin > 0 for every training sample whose
+ * bound is above 0, plus slack; recall = the fraction of zero-bound samples
+ * that margin leaves transparent. */
+int ivr_mlp_calibrate(ivr_mlp *mlp, float slack, float *margin, float *recall);
+/* Attaches a predictor and its margin to the volume (NULL detaches); the
+ * volume's learned grids are dropped.  The predictor must outlive the
+ * attachment; changing its parameters later invalidates the grids too.
+ * certify != 0: each learned grid is checked cell by cell against the exact
+ * empty-cell test as it is built, and a false skip (a cell called
+ * transparent whose LUT range holds a nonzero opacity) is kept opaque.
+ * With certify = 0 only the per-frame image judge guards the frames. */
+int ivr_volume_set_mlp(ivr_volume *vol, ivr_mlp *mlp, float margin, int certify);
+/* Counts over the learned grids built since ivr_volume_set_mlp (waits):
+ * stats[0] cells, [1] exactly transparent cells, [2] cells the predictor
+ * called transparent, [3] false skips among them. */
+int ivr_volume_learned_stats(ivr_volume *vol, unsigned long long *stats);
+/* The judge's totals over the view's learned-skip frames (waits for them). */
+int ivr_view_judge_stats(ivr_view *view, ivr_judge_stats *stats);
 
 /* --- compositing and output -------------------------------------------- */
 /* compositetiles (main.c:1203-1218): num sub-images of w*h RGBA floats in

@@ -29,7 +29,25 @@ class RenderParams(ctypes.Structure):
         ("skip", ctypes.c_int),
         ("tilew", ctypes.c_int),
         ("tileh", ctypes.c_int),
+        ("judge_stride", ctypes.c_int),
+        ("judge_tol", ctypes.c_int),
     ]
+
+
+class JudgeStats(ctypes.Structure):
+    _fields_ = [
+        ("frames", ctypes.c_ulonglong),
+        ("fallbacks", ctypes.c_ulonglong),
+        ("pixels", ctypes.c_ulonglong),
+        ("worst", ctypes.c_int),
+        ("pad", ctypes.c_int),
+        ("exact_frames", ctypes.c_ulonglong),
+    ]
+
+
+MLP_PARAMS = 6337
+MLP_IN = 32
+MLP_TRANSPARENT = 0.5
 
 
 class ServerConfig(ctypes.Structure):
@@ -134,6 +152,22 @@ SIGNATURES = {
     "ivr_server_listen": (_I, [_P, _I, _I, _I, ctypes.POINTER(_I)]),
     "ivr_server_times": (_I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                               ctypes.POINTER(ctypes.c_double)]),
+    "ivr_mlp_create": (_I, [_P, ctypes.c_ulonglong, ctypes.POINTER(_P)]),
+    "ivr_mlp_free": (_I, [_P]),
+    "ivr_mlp_get_params": (_I, [_P, _PF]),
+    "ivr_mlp_set_params": (_I, [_P, _PF]),
+    "ivr_mlp_save": (_I, [_P, ctypes.c_char_p]),
+    "ivr_mlp_load": (_I, [_P, ctypes.c_char_p]),
+    "ivr_mlp_features": (_I, [_P, _P, _P, _P, _P, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong), _P]),
+    "ivr_mlp_forward": (_I, [_P, _P, ctypes.c_longlong, _P, _P]),
+    "ivr_mlp_gradient": (_I, [_P, _P, _P, ctypes.c_longlong, _F, _P, _P, _P]),
+    "ivr_mlp_add_samples": (_I, [_P, _P, _P, ctypes.POINTER(ctypes.c_longlong)]),
+    "ivr_mlp_clear_samples": (_I, [_P]),
+    "ivr_mlp_train": (_I, [_P, _I, _I, _F, _F, _PF]),
+    "ivr_mlp_calibrate": (_I, [_P, _F, _PF, _PF]),
+    "ivr_volume_set_mlp": (_I, [_P, _P, _F, _I]),
+    "ivr_view_judge_stats": (_I, [_P, ctypes.POINTER(JudgeStats)]),
+    "ivr_volume_learned_stats": (_I, [_P, ctypes.POINTER(ctypes.c_ulonglong)]),
     "ivr_composite": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "ivr_quantize": (_I, [_P, _P, _P, ctypes.c_longlong, _P]),
 }

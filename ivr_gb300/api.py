@@ -22,7 +22,8 @@ TF_SEISMIC, TF_MED, TF_SEISMIC2, TF_CHEM, TF_BLEND, TF_RGBBLEND, TF_F2B = range(
 CM_BASE, CM_RAINBOW, CM_MEDICAL, CM_SEISMIC, CM_JET, CM_NOMAP = 0, 1, 2, 3, 4, -1
 PRESET_REF, PRESET_CONFIG = 0, 1
 ORDER_CENTER, ORDER_AXIS = 0, 1
-SKIP_NONE, SKIP_GRID = 0, 1
+SKIP_NONE, SKIP_GRID, SKIP_LEARNED = 0, 1, 2
+MLP_PARAMS, MLP_IN, MLP_TRANSPARENT = _lib.MLP_PARAMS, _lib.MLP_IN, _lib.MLP_TRANSPARENT
 
 
 def _vp(x) -> Optional[int]:
@@ -37,14 +38,18 @@ def ref_params(tile=(1, 1)) -> RenderParams:
     return p
 
 
-def config_params(step=0.5, term_alpha=0.99, skip=True, tile=(1, 1)) -> RenderParams:
-    """Benchmark sampling: true trilinear, ``step`` voxels, early termination."""
+def config_params(step=0.5, term_alpha=0.99, skip=True, tile=(1, 1), judge_stride=16,
+                  judge_tol=1) -> RenderParams:
+    """Benchmark sampling: true trilinear, ``step`` voxels, early termination.
+    ``skip``: True/False for the exact grid or none, or a SKIP_* value
+    (SKIP_LEARNED judges 1 in ``judge_stride`` tiles at ``judge_tol``)."""
     p = RenderParams()
     _lib.load().ivr_params_config(ctypes.byref(p))
     p.step = step
     p.term_alpha = term_alpha
-    p.skip = SKIP_GRID if skip else SKIP_NONE
+    p.skip = (SKIP_GRID if skip else SKIP_NONE) if isinstance(skip, bool) else int(skip)
     p.tilew, p.tileh = tile
+    p.judge_stride, p.judge_tol = judge_stride, judge_tol
     return p
 
 
@@ -108,6 +113,12 @@ class Context:
         self.check(self.lib.ivr_view_create(self.h, ctypes.byref(out)))
         return View(self, out)
 
+    def mlp(self, seed: int = 0) -> "Mlp":
+        """A learned empty-space predictor (He-initialised)."""
+        h = ctypes.c_void_p()
+        self.check(self.lib.ivr_mlp_create(self.h, seed, ctypes.byref(h)))
+        return Mlp(self, h)
+
     def batch(self, max_frames: int) -> "Batch":
         out = ctypes.c_void_p()
         self.check(self.lib.ivr_batch_create(self.h, max_frames, ctypes.byref(out)))
@@ -140,6 +151,19 @@ class Volume:
         self.ctx.check(self.ctx.lib.ivr_volume_histogram(
             self.h, hist.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), hsize))
         return hist
+
+    def set_mlp(self, mlp: Optional["Mlp"], margin: float = 0.0, certify: bool = True) -> "Volume":
+        """Attaches the predictor used by SKIP_LEARNED views (None detaches);
+        ``certify`` checks each learned grid against the exact test as it is
+        built and keeps false skips opaque."""
+        self.ctx.check(self.ctx.lib.ivr_volume_set_mlp(self.h, mlp.h if mlp else None, margin, int(certify)))
+        return self
+
+    def learned_stats(self) -> dict:
+        """Cell counts over the learned grids built since set_mlp."""
+        st = (ctypes.c_ulonglong * 4)()
+        self.ctx.check(self.ctx.lib.ivr_volume_learned_stats(self.h, st))
+        return {"cells": st[0], "exact_transparent": st[1], "learned_transparent": st[2], "false_skips": st[3]}
 
     def free(self):
         if self.h:
@@ -210,6 +234,13 @@ class View:
                                                _vp(stream)))
         return {"lattice": a.value, "executed": e.value, "touched_bytes": t.value}
 
+    def judge_stats(self) -> dict:
+        """Totals of the learned-skip judge over this view's frames."""
+        st = _lib.JudgeStats()
+        self.ctx.check(self.ctx.lib.ivr_view_judge_stats(self.h, ctypes.byref(st)))
+        return {"frames": st.frames, "fallbacks": st.fallbacks, "pixels": st.pixels, "worst": st.worst,
+                "exact_frames": st.exact_frames}
+
     def render_host(self, vol: Volume, tf: TransferFunction, state: IvrState, params: RenderParams,
                     out: np.ndarray, stream=None):
         """End to end: STATE in, RGBA8 frame to host memory (out: uint8 [vh, vw, 4])."""
@@ -222,6 +253,73 @@ class View:
     def free(self):
         if self.h:
             self.ctx.lib.ivr_view_free(self.h)
+            self.h = None
+
+
+class Mlp:
+    """The learned empty-space predictor (ivr_mlp_*).  Device arrays are
+    integer addresses: features bf16 [n][MLP_IN] (uint16 storage), bounds
+    and predictions float32 [n]."""
+
+    def __init__(self, ctx: Context, h):
+        self.ctx, self.h = ctx, h
+
+    def _fp(self, a: np.ndarray):
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(MLP_PARAMS, dtype=np.float32)
+        self.ctx.check(self.ctx.lib.ivr_mlp_get_params(self.h, self._fp(p)))
+        return p
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        if p.size != MLP_PARAMS:
+            raise ValueError(f"{MLP_PARAMS} parameters expected")
+        self.ctx.check(self.ctx.lib.ivr_mlp_set_params(self.h, self._fp(p)))
+
+    def save(self, path: str):
+        self.ctx.check(self.ctx.lib.ivr_mlp_save(self.h, path.encode()))
+
+    def load(self, path: str):
+        self.ctx.check(self.ctx.lib.ivr_mlp_load(self.h, path.encode()))
+
+    def features(self, vol: Volume, tf: TransferFunction, x_dev, bound_dev, cap: int, stream=None) -> int:
+        n = ctypes.c_longlong()
+        self.ctx.check(self.ctx.lib.ivr_mlp_features(self.h, vol.h, tf.h, _vp(x_dev), _vp(bound_dev), cap,
+                                                     ctypes.byref(n), _vp(stream)))
+        return n.value
+
+    def forward(self, x_dev, n: int, y_dev, stream=None):
+        self.ctx.check(self.ctx.lib.ivr_mlp_forward(self.h, _vp(x_dev), n, _vp(y_dev), _vp(stream)))
+
+    def gradient(self, x_dev, bound_dev, n: int, wneg: float, grad_dev, loss_dev, stream=None):
+        self.ctx.check(self.ctx.lib.ivr_mlp_gradient(self.h, _vp(x_dev), _vp(bound_dev), n, wneg, _vp(grad_dev),
+                                                     _vp(loss_dev), _vp(stream)))
+
+    def add_samples(self, vol: Volume, tf: TransferFunction) -> int:
+        n = ctypes.c_longlong()
+        self.ctx.check(self.ctx.lib.ivr_mlp_add_samples(self.h, vol.h, tf.h, ctypes.byref(n)))
+        return n.value
+
+    def clear_samples(self):
+        self.ctx.check(self.ctx.lib.ivr_mlp_clear_samples(self.h))
+
+    def train(self, epochs: int, batch_rows: int = 8192, lr: float = 2e-3, wneg: float = 4.0) -> np.ndarray:
+        losses = np.zeros(epochs, dtype=np.float32)
+        self.ctx.check(self.ctx.lib.ivr_mlp_train(self.h, epochs, batch_rows, lr, wneg, self._fp(losses)))
+        return losses
+
+    def calibrate(self, slack: float = 0.02):
+        """(margin, recall): the margin that keeps every training cell with a
+        bound above 0 opaque, and the share of transparent cells it keeps."""
+        m, r = ctypes.c_float(), ctypes.c_float()
+        self.ctx.check(self.ctx.lib.ivr_mlp_calibrate(self.h, slack, ctypes.byref(m), ctypes.byref(r)))
+        return m.value, r.value
+
+    def free(self):
+        if self.h:
+            self.ctx.lib.ivr_mlp_free(self.h)
             self.h = None
 
 

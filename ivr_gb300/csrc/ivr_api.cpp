@@ -11,87 +11,9 @@
 #include <string>
 #include <vector>
 
-#include "ivr_frame.h"
+#include "ivr_handles.h"
 
-struct ivr_ctx {
-    int device = 0;
-    size_t budget = 0;   // 0 = unlimited
-    size_t used = 0;
-    std::string err;
-    unsigned long long *d_counters = nullptr;
-    float *d_partial = nullptr;  // min/max partials
-    uchar4 *d_frame8 = nullptr;  // ivr_render_host staging
-    size_t frame8_bytes = 0;
-    unsigned tf_serial = 0;
-    unsigned long long grid_clock = 0;  // recency of the per-TF distance fields
-};
-
-struct ivr_volume {
-    ivr_ctx *ctx = nullptr;
-    int w = 0, h = 0, d = 0, dtype = 0;
-    void *d_full = nullptr;
-    size_t full_bytes = 0;
-    std::vector<ivr::HostBrick> bricks;
-    int py = 1, px = 1, pz = 1, overlap = 0;
-    bool have_minmax = false;
-    float vmin = 0.0f, vmax = 0.0f;
-    // macrocell distance fields, one set per transfer function in use
-    // (keyed by TF serial and whether the opacity scale is zero)
-    struct TfGrid {
-        unsigned serial;
-        int zero_alpha;
-        unsigned long long last_use;  // ctx grid_clock
-        std::vector<uint8_t *> dist;  // per brick
-        cudaEvent_t ev;               // after the last launch that read it
-        cudaEvent_t built;            // after its build
-    };
-    std::vector<TfGrid *> grids;
-};
-constexpr size_t kMaxTfGrids = 128;
-
-struct ivr_tf {
-    ivr_ctx *ctx = nullptr;
-    int n = 0, off = 0, mode = IVR_TF_SEISMIC;
-    float scale = 1.0f;
-    float4 *d_lut = nullptr;
-    int *d_nzprefix = nullptr;
-    int cap = 0;
-    std::vector<float> host;
-    unsigned serial = 0;
-};
-
-struct ivr_view {
-    ivr_ctx *ctx = nullptr;
-    ivr_volume *vol = nullptr;
-    unsigned long long *d_tickets = nullptr;  // tile tickets of CONFIG launches
-    unsigned long long ticket_base = 0;
-    bool tickets_dirty = true;
-    ivr_render_params p{};
-    ivr_state st{};
-    bool valid = false;
-    ivr::FrameDesc f{};
-    ivr_frame_info info{};
-};
-
-struct ivr_batch {
-    ivr_ctx *ctx = nullptr;
-    int cap = 0, n = 0, dtype = -1;
-    int variant = 0;
-    void *h_buf = nullptr;  // pinned: BatchHeader then cap BatchItems
-    void *d_buf = nullptr;
-    size_t buf_bytes = 0;
-    unsigned long long *d_ticket = nullptr;
-    cudaEvent_t done = nullptr;  // after the last render: the staging may be refilled
-    bool pending = false;
-    cudaGraphExec_t graph[ivr::kBatchVariants] = {};
-    cudaStream_t graph_stream[ivr::kBatchVariants] = {};
-    std::vector<ivr_volume::TfGrid *> grids;  // read by the frames in the batch
-    unsigned long long clock0 = 0;           // grid_clock when it was cleared
-};
-
-namespace {
-
-using namespace ivr;
+namespace ivr {
 
 int fail(ivr_ctx *c, int code, const char *fmt, ...)
 {
@@ -110,12 +32,6 @@ int cuda_fail(ivr_ctx *c, cudaError_t e, const char *what)
 {
     return fail(c, IVR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
-
-#define CK(ctx, call)                                                   \
-    do {                                                                \
-        cudaError_t e_ = (call);                                        \
-        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call);      \
-    } while (0)
 
 int dev_alloc(ivr_ctx *c, size_t bytes, void **p)
 {
@@ -145,23 +61,49 @@ size_t brick_bytes(const ivr_volume *v, const HostBrick &b)
     return (size_t) b.lw * b.lh * b.ld * dtype_size(v->dtype);
 }
 
-size_t mc_cells(const HostBrick &b) { return (size_t) b.mcx * b.mcy * b.mcz; }
+}  // namespace ivr
+
+namespace {
+
+using namespace ivr;
+
+void delete_grid(ivr_volume *v, ivr_volume::TfGrid *g)
+{
+    for (size_t k = 0; k < g->dist.size(); k++)
+        if (g->dist[k]) dev_free(v->ctx, g->dist[k], mc_cells(v->bricks[k]));
+    if (g->ev) cudaEventDestroy(g->ev);
+    if (g->built) cudaEventDestroy(g->built);
+    if (g->h_reject) cudaFreeHost(g->h_reject);
+    if (g->d_bad) dev_free(v->ctx, g->d_bad, sizeof(int));
+    delete g;
+}
+
+}  // namespace
+
+void ivr::drop_learned_grids(ivr_volume *v)
+{
+    if (v->grids.empty()) return;
+    cudaDeviceSynchronize();
+    std::vector<ivr_volume::TfGrid *> keep;
+    for (auto *g : v->grids)
+        if (g->learned) delete_grid(v, g);
+        else keep.push_back(g);
+    v->grids.swap(keep);
+}
+
+namespace {
 
 void free_grids(ivr_volume *v)
 {
     if (!v->grids.empty()) cudaDeviceSynchronize();
-    for (auto *g : v->grids) {
-        for (size_t k = 0; k < g->dist.size(); k++) dev_free(v->ctx, g->dist[k], mc_cells(v->bricks[k]));
-        if (g->ev) cudaEventDestroy(g->ev);
-        if (g->built) cudaEventDestroy(g->built);
-        delete g;
-    }
+    for (auto *g : v->grids) delete_grid(v, g);
     v->grids.clear();
 }
 
 void free_bricks(ivr_volume *v)
 {
     free_grids(v);
+    learned_release(v);
     for (auto &b : v->bricks) {
         if (b.owns) dev_free(v->ctx, b.data, brick_bytes(v, b));
         dev_free(v->ctx, b.mc_minmax, mc_cells(b) * 2 * sizeof(float));
@@ -228,22 +170,33 @@ int valid_params(ivr_ctx *c, const ivr_render_params *p)
         if (p->max_samples != 0) return fail(c, IVR_ERR_UNSUPPORTED, "CONFIG samples are not capped");
     }
     if (p->tilew < 1 || p->tileh < 1) return fail(c, IVR_ERR_INVALID, "tile size must be >= 1");
+    if (p->skip < IVR_SKIP_NONE || p->skip > IVR_SKIP_LEARNED) return fail(c, IVR_ERR_INVALID, "unknown skip %d", p->skip);
+    if (p->skip == IVR_SKIP_LEARNED) {
+        if (p->preset != IVR_PRESET_CONFIG) return fail(c, IVR_ERR_UNSUPPORTED, "learned skipping needs the CONFIG preset");
+        if (p->judge_stride < 1 || p->judge_stride > (1 << 20))
+            return fail(c, IVR_ERR_INVALID, "judge_stride must be in [1, 2^20]");
+        if (p->judge_tol < 0 || p->judge_tol > 255) return fail(c, IVR_ERR_INVALID, "judge_tol must be in [0, 255]");
+    }
     return IVR_OK;
 }
 
 // The per-brick distance fields of the volume for a TF, built on `s` when
-// the TF (or a zero opacity scale) is new to the volume.  Up to kMaxTfGrids
-// are kept; beyond that the least recently used one not read by frames since
+// the TF (or a zero opacity scale) is new to the volume: the exact fields, or
+// with `learned` the attached predictor's.  Up to kMaxTfGrids are kept;
+// beyond that the least recently used one not read by frames since
 // `protect_from` is rebuilt in place once the last launch that read it has
 // finished (its event), or a new one is added when every grid is protected.
-int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s, unsigned long long protect_from,
-            ivr_volume::TfGrid **out, bool *built = nullptr)
+int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, bool learned, cudaStream_t s,
+            unsigned long long protect_from, ivr_volume::TfGrid **out, bool *built = nullptr)
 {
     if (built) *built = false;
     ivr_ctx *c = v->ctx;
+    if (learned && !v->mlp) return fail(c, IVR_ERR_INVALID, "IVR_SKIP_LEARNED: no predictor attached to the volume");
+    const unsigned mser = learned ? mlp_serial(v->mlp) : 0;
     const unsigned long long now = ++c->grid_clock;
     for (auto *g : v->grids)
-        if (g->serial == tf->serial && g->zero_alpha == (int) zero_alpha) {
+        if (g->serial == tf->serial && g->zero_alpha == (int) zero_alpha && g->learned == (int) learned &&
+            g->mlp_serial == mser) {
             g->last_use = now;
             *out = g;
             return IVR_OK;
@@ -255,31 +208,48 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s, un
     if (g) {
         CK(c, cudaEventSynchronize(g->ev));
     } else {
-        g = new ivr_volume::TfGrid{0, 0, 0, std::vector<uint8_t *>(v->bricks.size(), nullptr), nullptr, nullptr};
+        g = new ivr_volume::TfGrid();
+        g->dist.assign(v->bricks.size(), nullptr);
         int rc = IVR_OK;
         if (cudaEventCreateWithFlags(&g->ev, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&g->built, cudaEventDisableTiming) != cudaSuccess)
+            cudaEventCreateWithFlags(&g->built, cudaEventDisableTiming) != cudaSuccess ||
+            cudaHostAlloc((void **) &g->h_reject, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **) &g->d_reject, g->h_reject, 0) != cudaSuccess) {
+            cudaGetLastError();
             rc = IVR_ERR_CUDA;
+        }
+        if (rc == IVR_OK) rc = dev_alloc(c, sizeof(int), (void **) &g->d_bad);
         for (size_t k = 0; k < v->bricks.size() && rc == IVR_OK; k++)
             rc = dev_alloc(c, mc_cells(v->bricks[k]), (void **) &g->dist[k]);
         if (rc) {
-            for (size_t k = 0; k < v->bricks.size(); k++)
-                if (g->dist[k]) dev_free(c, g->dist[k], mc_cells(v->bricks[k]));
-            if (g->ev) cudaEventDestroy(g->ev);
-            if (g->built) cudaEventDestroy(g->built);
-            delete g;
-            return rc == IVR_ERR_CUDA ? fail(c, rc, "event for a distance field") : rc;
+            delete_grid(v, g);
+            return rc == IVR_ERR_CUDA ? fail(c, rc, "events for a distance field") : rc;
         }
         v->grids.push_back(g);
     }
     g->serial = tf->serial;
     g->zero_alpha = (int) zero_alpha;
+    g->learned = (int) learned;
+    g->mlp_serial = mser;
     g->last_use = now;
-    for (size_t k = 0; k < v->bricks.size(); k++) {
-        const HostBrick &b = v->bricks[k];
-        if (zero_alpha) CK(c, cudaMemsetAsync(g->dist[k], kDistCap, mc_cells(b), s));
-        else CK(c, launch_empty_flags(b.mc_minmax, b.mcx, b.mcy, b.mcz, tf->d_nzprefix, tf->n, tf->off, tf->scale,
-                                      g->dist[k], s));
+    g->rejected = false;
+    *(volatile int *) g->h_reject = 0;  // no launch that reads it is pending
+    CK(c, cudaMemsetAsync(g->d_bad, 0, sizeof(int), s));
+    if (zero_alpha) {
+        for (size_t k = 0; k < v->bricks.size(); k++) CK(c, cudaMemsetAsync(g->dist[k], kDistCap, mc_cells(v->bricks[k]), s));
+    } else if (learned) {
+        int rc = learned_fields(v, tf, g->dist, s);
+        if (rc) {
+            g->serial = 0;  // unusable; rebuilt on next use
+            g->last_use = 0;
+            return rc;
+        }
+    } else {
+        for (size_t k = 0; k < v->bricks.size(); k++) {
+            const HostBrick &b = v->bricks[k];
+            CK(c, launch_empty_flags(b.mc_minmax, b.mcx, b.mcy, b.mcz, tf->d_nzprefix, tf->n, tf->off, tf->scale,
+                                     g->dist[k], s));
+        }
     }
     CK(c, cudaEventRecord(g->ev, s));
     CK(c, cudaEventRecord(g->built, s));
@@ -288,13 +258,24 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, cudaStream_t s, un
     return IVR_OK;
 }
 
+// A learned grid the judge rejected is replaced by the exact one.  The host
+// reads the mapped verdict word without waiting: a verdict that has not
+// arrived yet only means one more judged frame.
+bool learned_rejected(ivr_volume::TfGrid *g)
+{
+    if (!g->rejected) g->rejected = *(volatile int *) g->h_reject != 0;
+    return g->rejected;
+}
+
 // Fills everything of a launch's frame descriptor that depends on the TF,
 // the output window and the skipping grid.
 int frame_for(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single, cudaStream_t s, FrameDesc &f,
-              ivr_volume::TfGrid **grid, unsigned long long protect_from = ~0ull, bool *built = nullptr)
+              ivr_volume::TfGrid **grid, unsigned long long protect_from = ~0ull, bool *built = nullptr,
+              ivr_volume::TfGrid **exact = nullptr)
 {
     if (built) *built = false;
     *grid = nullptr;
+    if (exact) *exact = nullptr;
     ivr_ctx *c = view->ctx;
     if (!view->valid) return fail(c, IVR_ERR_INVALID, "ivr_set_view has not succeeded on this view");
     if (!tf) return fail(c, IVR_ERR_INVALID, "null transfer function");
@@ -314,29 +295,38 @@ int frame_for(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single
     f.out_x = x; f.out_y = y; f.out_w = w; f.out_h = h;
     f.single = single;
     f.counters = nullptr;
-    if (view->p.skip == IVR_SKIP_GRID && view->p.preset == IVR_PRESET_CONFIG) {
-        int rc = tf_grid(view->vol, tf, !(f.alpha != 0.0f), s, protect_from, grid, built);
+    f.gate = nullptr;
+    f.judge = nullptr;
+    f.judge_reject = nullptr;
+    f.learned_bad = nullptr;
+    if (view->p.skip != IVR_SKIP_NONE && view->p.preset == IVR_PRESET_CONFIG) {
+        // a learned grid comes with the exact one (the judge's and the
+        // fallback's), unless the judge has rejected it: then only the exact
+        const bool zero_alpha = !(f.alpha != 0.0f);
+        bool learned = view->p.skip == IVR_SKIP_LEARNED && !zero_alpha;
+        ivr_volume::TfGrid *lg = nullptr;
+        if (learned) {
+            if (!exact) return fail(view->ctx, IVR_ERR_UNSUPPORTED, "IVR_SKIP_LEARNED frames render through ivr_render*");
+            int rc = tf_grid(view->vol, tf, false, true, s, protect_from, &lg, built);
+            if (rc) return rc;
+            learned = !learned_rejected(lg);
+        }
+        ivr_volume::TfGrid *eg = nullptr;
+        bool ebuilt = false;
+        int rc = tf_grid(view->vol, tf, zero_alpha, false, s, protect_from, &eg, &ebuilt);
         if (rc) return rc;
+        if (built) *built |= ebuilt;
+        *grid = learned ? lg : eg;
+        if (learned) *exact = eg;
         for (int k = 0; k < f.nb; k++) f.b[k].empty = (*grid)->dist[k];
     }
     return IVR_OK;
 }
 
-int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single, float *o32, uint8_t *o8,
-                  void *stream, std::vector<uint8_t *> *touched = nullptr)
+// One CONFIG/REF launch of f on the view's ticket counter.
+int launch_view(ivr_view *view, FrameDesc &f, float *o32, uint8_t *o8, cudaStream_t s)
 {
-    ivr_ctx *c = view ? view->ctx : nullptr;
-    if (!view) return fail(c, IVR_ERR_INVALID, "null view");
-    cudaStream_t s = (cudaStream_t) stream;
-    FrameDesc f;
-    ivr_volume::TfGrid *grid = nullptr;
-    int rc = frame_for(view, tf, x, y, w, h, single, s, f, &grid, c->grid_clock + 1);
-    if (rc) return rc;
-    if (touched) f.counters = c->d_counters;  // census launches count
-    if (touched) {
-        f.census = 1;
-        for (int k = 0; k < f.nb; k++) f.b[k].touched = (*touched)[k];
-    }
+    ivr_ctx *c = view->ctx;
     if (view->tickets_dirty) {
         CK(c, cudaMemsetAsync(view->d_tickets, 0, sizeof(unsigned long long), s));
         view->ticket_base = 0;
@@ -351,7 +341,49 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
         return cuda_fail(c, e, "march launch");
     }
     view->ticket_base += (unsigned long long) used;
+    return IVR_OK;
+}
+
+int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single, float *o32, uint8_t *o8,
+                  void *stream, std::vector<uint8_t *> *touched = nullptr)
+{
+    ivr_ctx *c = view ? view->ctx : nullptr;
+    if (!view) return fail(c, IVR_ERR_INVALID, "null view");
+    cudaStream_t s = (cudaStream_t) stream;
+    FrameDesc f;
+    ivr_volume::TfGrid *grid = nullptr, *exact = nullptr;
+    int rc = frame_for(view, tf, x, y, w, h, single, s, f, &grid, c->grid_clock + 1, nullptr, &exact);
+    if (rc) return rc;
+    if (touched) {
+        f.counters = c->d_counters;  // census launches count
+        f.census = 1;
+        for (int k = 0; k < f.nb; k++) f.b[k].touched = (*touched)[k];
+    }
+    // a learned-skip frame: judged in the same launch (a rotating
+    // 1/judge_stride of its tiles marched again with the exact grid), then
+    // re-rendered with the exact grid by a launch gated on the verdict
+    const bool judged = exact && !touched && (o32 || o8);
+    if (judged) {
+        f.judge = (JudgeWords *) view->d_judge;
+        f.judge_reject = grid->d_reject;
+        f.learned_bad = grid->d_bad;
+        f.judge_stride = view->p.judge_stride;
+        f.judge_phase = (int) (view->judge_frame++ % (unsigned long long) view->p.judge_stride);
+        f.judge_tol = view->p.judge_tol;
+        for (int k = 0; k < f.nb; k++) f.exact[k] = exact->dist[k];
+    }
+    rc = launch_view(view, f, o32, o8, s);
+    if (rc) return rc;
+    if (judged) {
+        FrameDesc ff = f;
+        ff.judge = nullptr;
+        for (int k = 0; k < ff.nb; k++) ff.b[k].empty = exact->dist[k];
+        ff.gate = &((JudgeWords *) view->d_judge)->fail;
+        rc = launch_view(view, ff, o32, o8, s);
+        if (rc) return rc;
+    }
     if (grid) CK(c, cudaEventRecord(grid->ev, s));
+    if (exact) CK(c, cudaEventRecord(exact->ev, s));
     return IVR_OK;
 }
 
@@ -370,6 +402,8 @@ void ivr_params_ref(ivr_render_params *p)
     p->skip = IVR_SKIP_NONE;
     p->tilew = 1;
     p->tileh = 1;
+    p->judge_stride = 16;
+    p->judge_tol = 1;
 }
 
 void ivr_params_config(ivr_render_params *p)
@@ -383,6 +417,8 @@ void ivr_params_config(ivr_render_params *p)
     p->skip = IVR_SKIP_GRID;
     p->tilew = 1;
     p->tileh = 1;
+    p->judge_stride = 16;
+    p->judge_tol = 1;
 }
 
 int ivr_create(int device, size_t budget, ivr_ctx **out)
@@ -494,6 +530,7 @@ int ivr_volume_free(ivr_volume *v)
 {
     if (!v) return IVR_ERR_INVALID;
     free_bricks(v);
+    dev_free(v->ctx, v->d_lstats, 4 * sizeof(unsigned long long));
     dev_free(v->ctx, v->d_full, v->full_bytes);
     delete v;
     return IVR_OK;
@@ -651,8 +688,10 @@ int ivr_view_create(ivr_ctx *c, ivr_view **out)
     ivr_view *v = new ivr_view();
     v->ctx = c;
     int rc = dev_alloc(c, sizeof(unsigned long long), (void **) &v->d_tickets);
+    if (rc == IVR_OK) rc = dev_alloc(c, sizeof(JudgeWords), (void **) &v->d_judge);
+    if (rc == IVR_OK && cudaMemset(v->d_judge, 0, sizeof(JudgeWords)) != cudaSuccess) rc = fail(c, IVR_ERR_CUDA, "judge words");
     if (rc) {
-        delete v;
+        ivr_view_free(v);
         return rc;
     }
     *out = v;
@@ -663,7 +702,23 @@ int ivr_view_free(ivr_view *v)
 {
     if (!v) return IVR_ERR_INVALID;
     dev_free(v->ctx, v->d_tickets, sizeof(unsigned long long));
+    dev_free(v->ctx, v->d_judge, sizeof(JudgeWords));
     delete v;
+    return IVR_OK;
+}
+
+int ivr_view_judge_stats(ivr_view *v, ivr_judge_stats *st)
+{
+    if (!v || !st) return v ? fail(v->ctx, IVR_ERR_INVALID, "null stats") : IVR_ERR_INVALID;
+    JudgeWords jw;
+    CK(v->ctx, cudaDeviceSynchronize());
+    CK(v->ctx, cudaMemcpy(&jw, v->d_judge, sizeof(jw), cudaMemcpyDeviceToHost));
+    memset(st, 0, sizeof(*st));
+    st->frames = jw.frames;
+    st->fallbacks = jw.fallbacks;
+    st->pixels = jw.pixels;
+    st->worst = jw.worst;
+    st->exact_frames = jw.exact_frames;
     return IVR_OK;
 }
 

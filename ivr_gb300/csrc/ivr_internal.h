@@ -32,6 +32,21 @@ struct DevBrick {
     uint8_t *touched;       // census only: cells an executed sample read
 };
 
+// Learned-skip judge words of a view (device).  maxdiff and warps_done are
+// per-frame scratch the judged launch clears after use; fail is the last
+// frame's verdict (the fallback launch's gate); the rest are running totals.
+struct JudgeWords {
+    int maxdiff;
+    int warps_done;
+    int fail;
+    int worst;                      // largest difference seen
+    unsigned long long frames;      // frames judged
+    unsigned long long fallbacks;   // frames re-rendered with the exact grid
+    unsigned long long pixels;      // pixels compared
+    unsigned long long exact_frames;  // judged launches that found their learned
+                                      // grid marked wrong and used the exact one
+};
+
 // Everything one launch needs, passed by value as a __grid_constant__.
 struct FrameDesc {
     int vw, vh;              // viewport
@@ -58,8 +73,19 @@ struct FrameDesc {
                              // mark touched cells (diagnostic launch)
     unsigned long long *tickets;     // CONFIG: tile ticket counter (view-owned)
     unsigned long long ticket_base;  // its value when this launch starts
+    const int *gate;                 // CONFIG: if set, render only when
+                                     // *gate != 0 (the judge's fallback)
+    // CONFIG learned skipping (judge null: none): tiles whose index is
+    // judge_phase modulo judge_stride are marched again with the exact
+    // grids and compared; see JudgeWords
+    JudgeWords *judge;
+    int *judge_reject;               // set to 1 when the frame fails (host-mapped)
+    int *learned_bad;                // nonzero: the learned grid is wrong,
+                                     // render with the exact grids
+    int judge_stride, judge_phase, judge_tol;
     int order[kMaxBricks];   // near -> far
     DevBrick b[kMaxBricks];
+    const uint8_t *exact[kMaxBricks];  // the exact grids (judged launches)
 };
 
 // kernel parameters are limited to 32764 bytes
@@ -123,6 +149,8 @@ cudaError_t noalloc_histogram(const void *data, int dtype, long long n, int hsiz
 // *tickets: how many tile tickets the launch takes from f.tickets (a
 // persistent CONFIG launch takes each tile once and each warp fails once).
 cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s, long long *tickets);
+// transparent-radius relaxation of a flag grid (kDistCap or 0 per cell)
+cudaError_t launch_dist_relax(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s);
 // batched CONFIG frames of one volume dtype; *ticket must be zero at launch
 cudaError_t launch_batch(int dtype, int variant, const BatchHeader *hdr, const BatchItem *items,
                          unsigned long long *ticket, cudaStream_t s);

@@ -371,8 +371,14 @@ cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const
 {
     const int ncell = mcx * mcy * mcz;
     empty_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mc, ncell, nzprefix, lut_n, lut_off, lut_scale, empty);
+    return launch_dist_relax(empty, mcx, mcy, mcz, s);
+}
+
+cudaError_t launch_dist_relax(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s)
+{
+    const int ncell = mcx * mcy * mcz;
     for (int it = 0; it < kDistCap; it++)
-        dist_relax_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(empty, mcx, mcy, mcz);
+        dist_relax_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(dist, mcx, mcy, mcz);
     return cudaGetLastError();
 }
 

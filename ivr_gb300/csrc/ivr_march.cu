@@ -26,6 +26,8 @@ constexpr bool kPair = IVR_CFG_PAIR != 0;
 #endif
 // resident blocks per SM the CONFIG kernel is compiled for (8 = 64 registers)
 constexpr int kCfgBlocksPerSm = IVR_CFG_BLOCKS_PER_SM;
+// judged launches (learned skipping) hold the exact march's state as well
+constexpr int kJudgeBlocksPerSm = 7;
 // the batched kernel reads its frame from global memory and needs more
 // registers: 6 blocks (80 registers) per SM
 constexpr int kBatchBlocksPerSm = 6;
@@ -307,8 +309,8 @@ __device__ __forceinline__ int cfg_first_ge(float t0, float dt, float idt, float
 // samples are taken up to one past the exit without further checks.  Every
 // sample that is taken is computed exactly as without skipping.
 template <int DT, bool SKIP, bool CENSUS, bool PAIR>
-__device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float dy, float dz, float idx,
-                          float idy, float idz, float t0, float dt, float idt, float4 &acc, bool &done,
+__device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *empty, float dx, float dy, float dz,
+                          float idx, float idy, float idz, float t0, float dt, float idt, float4 &acc, bool &done,
                           unsigned long long &nexec, unsigned long long &nlat)
 {
     float tin, tout;
@@ -330,7 +332,7 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, float dx, float
             const int ci = min(max(__float2int_rd((y - b.bminy) * b.icy), 0), b.ny - 2) / kCell;
             const int ck = min(max(__float2int_rd((z - b.bminz) * b.icz), 0), b.nz - 2) / kCell;
             // r >= 1: the cube of cells within r-1 of this one is transparent
-            const int r = b.empty[((long long) ck * b.mcy + ci) * b.mcx + cj];
+            const int r = empty[((long long) ck * b.mcy + ci) * b.mcx + cj];
             const int rr = max(r, 1);
             // ray parameter where it leaves that cube (or this one opaque
             // cell); approximate, the margins absorb its rounding
@@ -466,10 +468,11 @@ __global__ void __launch_bounds__(kThreads) march_ref_kernel(const __grid_consta
     count_exec(f, nexec);
 }
 
-// One CONFIG ray: pixel (i, j) of the viewport, all bricks front to back.
+// One CONFIG ray: pixel (i, j) of the viewport, all bricks front to back,
+// skipping by the bricks' grids, or by the exact grids f.exact when exact.
 template <int DT, bool SKIP, bool CENSUS, bool PAIR>
 __device__ __forceinline__ float4 ray_cfg(const FrameDesc &f, int i, int j, unsigned long long &nexec,
-                                          unsigned long long &nlat)
+                                          unsigned long long &nlat, bool exact = false)
 {
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     bool any = false;
@@ -493,61 +496,128 @@ __device__ __forceinline__ float4 ray_cfg(const FrameDesc &f, int i, int j, unsi
         if (f.single >= 0 && k != f.single) continue;
         const DevBrick &b = f.b[k];
         if (!in_rect(b, i, j)) continue;
-        if (SKIP && b.empty != nullptr)
-            march_cfg<DT, true, CENSUS, PAIR>(f, b, dx, dy, dz, idx, idy, idz, t0, dt, idt, acc, done, nexec, nlat);
+        const uint8_t *empty = exact ? f.exact[k] : b.empty;
+        if (SKIP && empty != nullptr)
+            march_cfg<DT, true, CENSUS, PAIR>(f, b, empty, dx, dy, dz, idx, idy, idz, t0, dt, idt, acc, done, nexec,
+                                              nlat);
         else
-            march_cfg<DT, false, CENSUS, PAIR>(f, b, dx, dy, dz, idx, idy, idz, t0, dt, idt, acc, done, nexec, nlat);
+            march_cfg<DT, false, CENSUS, PAIR>(f, b, empty, dx, dy, dz, idx, idy, idz, t0, dt, idt, acc, done, nexec,
+                                               nlat);
     }
     return acc;
 }
 
-// Persistent CONFIG kernel: every warp takes 8x4 pixel tiles from a ticket
-// counter until none are left, so warps that drew short rays pick up more
-// work instead of idling while the grid's last blocks finish.
-#ifndef IVR_CFG_PERSISTENT
-#define IVR_CFG_PERSISTENT 1
-#endif
-
 // One pixel of the output window (ow, oh) = (oj, oi).
 template <int DT, bool SKIP, bool CENSUS, bool PAIR>
-__device__ __forceinline__ void pixel_cfg(const FrameDesc &f, int oi, int oj, float4 *out32, uchar4 *out8,
-                                          unsigned long long &nexec, unsigned long long &nlat)
+__device__ __forceinline__ float4 pixel_cfg(const FrameDesc &f, int oi, int oj, float4 *out32, uchar4 *out8,
+                                            unsigned long long &nexec, unsigned long long &nlat, bool exact = false)
 {
-    if (oj >= f.out_w || oi >= f.out_h) return;
-    const int j = f.out_x + oj, i = f.out_y + oi;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (i < f.vh && j < f.vw) acc = ray_cfg<DT, SKIP, CENSUS, PAIR>(f, i, j, nexec, nlat);
+    if (oj >= f.out_w || oi >= f.out_h) return acc;
+    const int j = f.out_x + oj, i = f.out_y + oi;
+    if (i < f.vh && j < f.vw) acc = ray_cfg<DT, SKIP, CENSUS, PAIR>(f, i, j, nexec, nlat, exact);
     const long long o = (long long) oi * f.out_w + oj;
     if (out32) out32[o] = acc;
     if (out8) out8[o] = make_uchar4(q8(acc.x), q8(acc.y), q8(acc.z), q8(acc.w));
+    return acc;
 }
 
-// CONFIG kernel.  Persistent form: every warp takes 8x4 pixel tiles from a
-// ticket counter until none are left, so warps that drew short rays pick up
-// more work instead of idling while the grid's last blocks finish.  Grid
-// form: one thread per pixel, blocks of 2x2 warp tiles.
-template <int DT, bool SKIP, bool CENSUS>
-__global__ void __launch_bounds__(kThreads, kCfgBlocksPerSm) march_cfg_kernel(const __grid_constant__ FrameDesc f,
+// Largest channel difference between a pixel this thread stored (out8, or
+// out32 quantised) and the exact march's colour.
+__device__ __forceinline__ int q8_diff(const uchar4 *out8, const float4 *out32, long long o, float4 b)
+{
+    uchar4 a;
+    if (out8) {
+        a = out8[o];
+    } else {
+        const float4 v = out32[o];
+        a = make_uchar4(q8(v.x), q8(v.y), q8(v.z), q8(v.w));
+    }
+    const int dx = abs((int) a.x - (int) q8(b.x)), dy = abs((int) a.y - (int) q8(b.y));
+    const int dz = abs((int) a.z - (int) q8(b.z)), dw = abs((int) a.w - (int) q8(b.w));
+    return max(max(dx, dy), max(dz, dw));
+}
+
+// End of a judged launch for one warp: its largest difference and pixel
+// count go into the judge words; the launch's last warp sets the verdict
+// (fail = largest difference > tolerance), adds it to the totals, marks the
+// learned grid rejected on failure and clears the per-frame words.
+__device__ __forceinline__ void judge_finish(const FrameDesc &f, int worst, unsigned judged, bool exact)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+        judged += __shfl_xor_sync(0xffffffffu, judged, o);
+    }
+    if ((threadIdx.x & 31) != 0) return;
+    JudgeWords *jw = f.judge;
+    if (worst > 0) atomicMax(&jw->maxdiff, worst);
+    if (judged) atomicAdd(&jw->pixels, (unsigned long long) judged);
+    __threadfence();
+    const int warps = (int) gridDim.x * (int) (blockDim.x >> 5);
+    if (atomicAdd(&jw->warps_done, 1) != warps - 1) return;
+    __threadfence();
+    const int m = atomicAdd(&jw->maxdiff, 0);
+    const int failed = m > f.judge_tol;
+    jw->fail = failed;
+    if (exact) {
+        jw->exact_frames += 1;
+    } else {
+        jw->frames += 1;
+        jw->fallbacks += (unsigned long long) failed;
+        if (m > jw->worst) jw->worst = m;
+    }
+    if (failed) {
+        *f.learned_bad = 1;
+        *(volatile int *) f.judge_reject = 1;
+        __threadfence_system();
+    }
+    jw->maxdiff = 0;
+    jw->warps_done = 0;
+}
+
+// CONFIG kernel, persistent: every warp takes 8x4 pixel tiles from the
+// view's ticket counter until none are left, so warps that drew short rays
+// pick up more work instead of idling while the grid's last blocks finish.
+// A gated launch (f.gate set) renders only if *f.gate != 0; otherwise its
+// warps take their share of tickets (tiles + one failed take each) and leave.
+// JUDGE (learned skipping): every tile whose index is judge_phase modulo
+// judge_stride is marched a second time with the exact grids and the 8-bit
+// results compared (judge_finish); a learned grid already marked wrong
+// (*learned_bad) is not used: the launch marches with the exact grids.
+template <int DT, bool SKIP, bool CENSUS, bool JUDGE>
+__global__ void __launch_bounds__(kThreads, JUDGE ? kJudgeBlocksPerSm : kCfgBlocksPerSm)
+    march_cfg_kernel(const __grid_constant__ FrameDesc f,
                                                                               float4 *out32, uchar4 *out8)
 {
     unsigned long long nexec = 0, nlat = 0;
-#if IVR_CFG_PERSISTENT
     const int lane = threadIdx.x & 31;
     const int tiles_x = (f.out_w + 7) >> 3;
     const long long ntiles = (long long) tiles_x * ((f.out_h + 3) >> 2);
+    if (f.gate != nullptr && *f.gate == 0) {
+        const bool first = blockIdx.x == 0 && threadIdx.x == 0;
+        if (lane == 0) atomicAdd(f.tickets, first ? (unsigned long long) ntiles + 1ull : 1ull);
+        return;
+    }
+    int worst = 0;
+    unsigned judged = 0;
+    const bool exact = JUDGE && *(volatile const int *) f.learned_bad != 0;
     for (;;) {
         unsigned long long ticket = 0;
         if (lane == 0) ticket = atomicAdd(f.tickets, 1ull);
         const long long tile = (long long) (__shfl_sync(0xffffffffu, ticket, 0) - f.ticket_base);
         if (tile >= ntiles) break;
-        pixel_cfg<DT, SKIP, CENSUS, kPair>(f, (int) (tile / tiles_x) * 4 + (lane >> 3),
-                                           (int) (tile % tiles_x) * 8 + (lane & 7), out32, out8, nexec, nlat);
+        const int oi = (int) (tile / tiles_x) * 4 + (lane >> 3), oj = (int) (tile % tiles_x) * 8 + (lane & 7);
+        pixel_cfg<DT, SKIP, CENSUS, kPair>(f, oi, oj, out32, out8, nexec, nlat, exact);
+        if (JUDGE && !exact && tile % f.judge_stride == f.judge_phase) {
+            const int i = f.out_y + oi, j = f.out_x + oj;
+            if (oi < f.out_h && oj < f.out_w && i < f.vh && j < f.vw) {
+                const float4 ex = ray_cfg<DT, true, false, kPair>(f, i, j, nexec, nlat, true);
+                worst = max(worst, q8_diff(out8, out32, (long long) oi * f.out_w + oj, ex));
+                judged++;
+            }
+        }
     }
-#else
-    int i, j, oi, oj;
-    pixel_of(f, i, j, oi, oj);
-    pixel_cfg<DT, SKIP, CENSUS, kPair>(f, oi, oj, out32, out8, nexec, nlat);
-#endif
+    if (JUDGE) judge_finish(f, worst, judged, exact);
     if (CENSUS) count_exec(f, nexec, nlat);
 }
 
@@ -572,18 +642,18 @@ cudaError_t launch_dt(const FrameDesc &f, float4 *o32, uchar4 *o8, cudaStream_t 
     if (f.preset == IVR_PRESET_CONFIG) {
         bool skip = false;
         for (int k = 0; k < f.nb; k++) skip |= f.b[k].empty != nullptr;
-        auto kern = f.census ? (skip ? march_cfg_kernel<DT, true, true> : march_cfg_kernel<DT, false, true>)
-                             : (skip ? march_cfg_kernel<DT, true, false> : march_cfg_kernel<DT, false, false>);
-        const size_t smem = 0;
-#if IVR_CFG_PERSISTENT
-        const int blocks = persistent_grid(kern, smem);
+        const bool judge = f.judge != nullptr;
+        if (judge && (!skip || f.census || f.judge_stride < 1 || f.judge_phase < 0 || f.judge_phase >= f.judge_stride))
+            return cudaErrorInvalidValue;
+        auto kern = f.census ? (skip ? march_cfg_kernel<DT, true, true, false> : march_cfg_kernel<DT, false, true, false>)
+                    : judge  ? march_cfg_kernel<DT, true, false, true>
+                    : skip   ? march_cfg_kernel<DT, true, false, false>
+                             : march_cfg_kernel<DT, false, false, false>;
+        const int blocks = persistent_grid(kern, 0);
         // every tile is taken once and every warp ends on one failed take
         if (warps_launched)
             *warps_launched = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2) + (long long) blocks * (kThreads / 32);
-        kern<<<blocks, kThreads, smem, s>>>(f, o32, o8);
-#else
-        kern<<<grid, kThreads, smem, s>>>(f, o32, o8);
-#endif
+        kern<<<blocks, kThreads, 0, s>>>(f, o32, o8);
         return cudaGetLastError();
     }
     if (warps_launched) *warps_launched = 0;

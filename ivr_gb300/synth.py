@@ -25,9 +25,9 @@ DT_MAX = {"u8": 255.0, "u16": 65535.0, "f32": 255.0}
 NP_DT = {"u8": np.uint8, "u16": np.uint16, "f32": np.float32}
 
 
-def _blob_params(rng, n_blobs):
+def _blob_params(rng, n_blobs, sigma_scale=1.0):
     c = rng.uniform(0.2, 0.8, size=(n_blobs, 3))
-    s = rng.uniform(0.03, 0.12, size=n_blobs)
+    s = rng.uniform(0.03, 0.12, size=n_blobs) * sigma_scale
     a = rng.uniform(0.3, 1.0, size=n_blobs)
     return c, s, a
 
@@ -65,13 +65,16 @@ def _value_noise_np(rng, shape, octaves):
 
 
 def blob_volume(shape, n_blobs=8, seed=0, dtype="u8", noise=0.05, value_noise=0.0,
-                octaves=3, zero_fraction=0.0, cell=16, device=None):
+                octaves=3, zero_fraction=0.0, cell=16, device=None, sigma_scale=1.0):
     """Sum of Gaussian blobs, see the module docstring.  ``zero_fraction``
     zeroes every voxel below the threshold that makes that fraction of the
-    ``cell``^3 macrocells exactly zero."""
+    ``cell``^3 macrocells exactly zero.  ``sigma_scale`` multiplies every
+    blob's sigma: (8 / n_blobs)^(1/3) keeps hundreds of blobs from summing
+    to a saturated volume (whose cell maxima are all 1, leaving no threshold
+    for the zero cells)."""
     d, h, w = shape
     rng = np.random.default_rng(seed)
-    c, s, a = _blob_params(rng, n_blobs)
+    c, s, a = _blob_params(rng, n_blobs, sigma_scale)
     maxdim = float(max(shape))
     use_torch = device is not None
     if use_torch:
@@ -165,13 +168,17 @@ def ramp_tf(n=256):
     return np.stack([r, g, b, a], axis=1).astype(np.float32)
 
 
-def knot_tf(seed, n=256, knots=16, zero_frac=0.6):
+def knot_tf(seed, n=256, knots=16, zero_frac=0.6, zero_first=False):
     """Random piecewise-linear TF: 16 knots evenly spaced on [0,1], opacity
     knots uniform in [0,1] with ``zero_frac`` of them zeroed, colour from the
-    blue -> red hue ramp.  Returns (lut float32 (n,4), knot opacities (16,))."""
+    blue -> red hue ramp.  ``zero_first`` zeroes the first two knots: the
+    lowest fifteenth of the range, and with it the empty background, is
+    transparent.  Returns (lut float32 (n,4), knot opacities (16,))."""
     rng = np.random.default_rng(seed)
     ka = rng.uniform(0.0, 1.0, size=knots)
     ka[rng.uniform(size=knots) < zero_frac] = 0.0
+    if zero_first:
+        ka[:2] = 0.0
     kx = np.linspace(0.0, 1.0, knots)
     x = np.arange(n, dtype=np.float64) / (n - 1)
     a = np.interp(x, kx, ka)
