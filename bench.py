@@ -184,7 +184,8 @@ def cpu_baseline(wl, vol, states, budget_s=20.0, threads=0):
         rows += band
         nb += 1
         el = time.perf_counter() - t0
-        if el > budget_s or nb >= 16:
+        # at least one frame's worth of bands, then about half the budget
+        if nb >= 16 and (el > budget_s / 2 or nb >= 16 * len(states)):
             break
     fps = (rows / h) / el
     return {"value": fps, "unit": "frames/s", "cores": threads or cores, "kind": "port",
@@ -310,7 +311,7 @@ def run_batch(args):
     ctx.close()
 
 
-def run_serve(args):
+def run_serve(args, quiet=False):
     """configs[4]: the steering server under Poisson load."""
     import torch
     from ivr_gb300 import api, serve, synth
@@ -326,12 +327,15 @@ def run_serve(args):
         scales.append(256.0 / 65536.0 if dt == "u16" else 1.0)
         names.append("x".join(map(str, shape)) + " " + dt)
     resident = ctx.mem_used
-    srv = api.Server(ctx, slots=SERVE["slots"], max_batch_frames=SERVE["batch"], arena_mib=SERVE["arena_mib"])
+    slots = args.serve_slots or SERVE["slots"]
+    batch = args.serve_batch or SERVE["batch"]
+    srv = api.Server(ctx, slots=slots, max_batch_frames=batch, arena_mib=SERVE["arena_mib"])
     ids = [srv.add_volume(v) for v in vols]
-    serve.run(srv, ids, scales, duration=SERVE["warm"], clients=SERVE["clients"], rate=SERVE["rate"], seed=1)
+    rate = tuple(float(x) for x in args.serve_rate.split(",")) if args.serve_rate else SERVE["rate"]
+    serve.run(srv, ids, scales, duration=SERVE["warm"], clients=SERVE["clients"], rate=rate, seed=1)
     with ClockSampler(0) as clk:
         res, wall = serve.run(srv, ids, scales, duration=SERVE["duration"], clients=SERVE["clients"],
-                              rate=SERVE["rate"], seed=2)
+                              rate=rate, seed=2)
     stats = srv.stats()
     srv.close()
     ok = [r for r in res if r["status"] == 0]
@@ -343,23 +347,30 @@ def run_serve(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u16/f32",
         "data": "synthetic (seeded blobs; Poisson arrivals)",
         "config": {"workload": "serve_32", "volumes": names, "clients": SERVE["clients"],
-                   "rate_per_client": SERVE["rate"], "duration_s": SERVE["duration"],
+                   "rate_per_client": rate, "duration_s": SERVE["duration"],
                    "sizes": "uniform from 256^2, 512^2, 1024^2, 1280x720, 1920x1080",
-                   "tf_edit": "every 5th request per client", "slots": SERVE["slots"],
-                   "max_batch_frames": SERVE["batch"], "arena_mib": SERVE["arena_mib"],
+                   "tf_edit": "every 5th request per client", "slots": slots,
+                   "max_batch_frames": batch, "arena_mib": SERVE["arena_mib"],
                    "hbm_budget_gib": SERVE["budget_gib"], "resident_volume_bytes": resident},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "max": float(lat.max()), "from": "scheduled arrival to RGBA8 frame in host memory"},
+        "latency_parts_ms": {
+            k: {"p50": float(np.percentile(a, 50)), "p99": float(np.percentile(a, 99))}
+            for k, a in (("generator_late", np.array([r["late"] for r in ok]) * 1000.0),
+                         ("queued", np.array([r["t_queue"] for r in ok]) * 1000.0),
+                         ("batch_to_host", np.array([r["t_total"] - r["t_queue"] for r in ok]) * 1000.0))},
         "requests": len(res), "rejected": len(res) - len(ok),
         "rejected_status": sorted({r["status"] for r in res if r["status"] != 0}),
         "megapixels_per_s": px / wall / 1e6, "batches": stats["batches"],
         "server_seconds": {k: stats[k] for k in ("gpu_s", "dispatch_s", "finish_s")}, "wall_s": wall,
         "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
     for v in vols:
         v.free()
     ctx.close()
+    if not quiet:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def run_learned(args, quiet=False):
@@ -480,6 +491,18 @@ def run_learned(args, quiet=False):
     return line
 
 
+def _extra(fn, args, keys):
+    """A workload's line reduced to `keys`, or the error it raised."""
+    import torch
+    try:
+        full = fn(args, quiet=True)
+        return {k: full[k] for k in keys if k in full}
+    except Exception as e:  # reported in the line, not hidden
+        return {"error": f"{type(e).__name__}: {e}"}
+    finally:
+        torch.cuda.empty_cache()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -490,6 +513,11 @@ def main():
                     choices=sorted(WORKLOADS) + ["batch_64x4", "serve_32", "learned_1024"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--serve-slots", type=int, default=0)
+    ap.add_argument("--serve-batch", type=int, default=0)
+    ap.add_argument("--serve-rate", default="", help="per-client request rate range lo,hi (req/s)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload only: skip the learned-skip and serving summaries")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload == "batch_64x4":
@@ -589,6 +617,7 @@ def main():
     if rank == 0:
         kavg = statistics.mean(kern_ms)
         peak, how = peaks()
+        sample_peak = ctx.sample_peak(v.dtype, sp)
         alg_bytes = touched / args.steps + w * h * 4  # compulsory volume bytes + RGBA8 out, per launch
         achieved = alg_bytes / (kavg / 1000.0) / 1e9
         traffic = profiled_traffic()
@@ -609,14 +638,27 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_source": how,
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "note": "algorithmic bytes = macrocells an executed sample read + RGBA8 output"},
+            "sample_roofline": {"bound": "sampler", "achieved": executed / args.steps / (kavg / 1000.0) / 1e9,
+                                "peak": sample_peak, "unit": "Gsamples/s",
+                                "frac": executed / args.steps / (kavg / 1000.0) / 1e9 / sample_peak,
+                                "note": "executed samples/s of the render launch against ivr_sample_peak: the "
+                                        "same sampler, LUT fetch and blend alone on a cache-resident brick"},
             "gpu_launches": args.steps,
             "clocks": clk.summary(),
         }
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(wl, vol, states[args.warmup:], budget_s=args.cpu_budget)
-        print(json.dumps(line), flush=True)
     v.free()
     ctx.close()
+    if rank == 0 and world == 1 and args.workload == "sorted_brick_512" and not args.no_extras:
+        # the metric's other two parts, each from its own workload
+        line["learned_skip"] = _extra(run_learned, args, ["fps", "speedup", "max_abs_diff_8bit_vs_plain",
+                                                          "gsamples_per_s", "learned_grid", "judge", "training",
+                                                          "first_frame_ms_median", "config", "clocks"])
+        line["serving"] = _extra(run_serve, args, ["value", "unit", "latency_ms", "requests", "rejected",
+                                                   "megapixels_per_s", "config", "clocks"])
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
 

@@ -132,6 +132,11 @@ int ivr_mem_used(const ivr_ctx *ctx, size_t *bytes);
  * output buffers); free with the same size. */
 int ivr_device_alloc(ivr_ctx *ctx, size_t bytes, void **ptr);
 int ivr_device_free(ivr_ctx *ctx, void *ptr, size_t bytes);
+/* Page-locked host memory (not counted against the budget), for frame
+ * buffers the device copies into directly: ivr_server requests whose
+ * rgba8_host lies in it skip the server's staging copy. */
+int ivr_host_alloc(ivr_ctx *ctx, size_t bytes, void **ptr);
+int ivr_host_free(ivr_ctx *ctx, void *ptr);  /* ctx may be NULL (no message then) */
 
 /* --- volume load / brick setup (readvoldata, readfromfile, initvolbbox) -- */
 /* Copies a host volume (x fastest, [d][h][w]) to the device.  byteswap != 0
@@ -257,7 +262,8 @@ typedef struct ivr_request {
     int volume;               /* id from ivr_server_add_volume */
     int tf;                   /* id from ivr_server_add_tf */
     ivr_state state;          /* the steering STATE: view, window, opacity, clip */
-    uint8_t *rgba8_host;      /* viewport RGBA8, written before completion */
+    uint8_t *rgba8_host;      /* viewport RGBA8, written before completion (page-locked
+                                 memory, e.g. from ivr_host_alloc, is written directly) */
     unsigned long long tag;   /* the caller's id, returned in the completion */
 } ivr_request;
 typedef struct ivr_completion {
@@ -363,6 +369,14 @@ int ivr_volume_set_mlp(ivr_volume *vol, ivr_mlp *mlp, float margin, int certify)
 int ivr_volume_learned_stats(ivr_volume *vol, unsigned long long *stats);
 /* The judge's totals over the view's learned-skip frames (waits for them). */
 int ivr_view_judge_stats(ivr_view *view, ivr_judge_stats *stats);
+
+/* --- measurement -------------------------------------------------------- */
+/* The sample-rate roofline of the CONFIG march (no counterpart in the
+ * reference): the sampler alone -- trilinear reconstruction, LUT fetch,
+ * front-to-back blend, no ray set-up, skipping or divergence -- on a 64^3
+ * brick of `dtype` that stays in cache, every resident thread marching its
+ * own ray.  Samples per second / 1e9 (waits for the timing). */
+int ivr_sample_peak(ivr_ctx *ctx, int dtype, double *gsamples_per_s, void *stream);
 
 /* --- compositing and output -------------------------------------------- */
 /* compositetiles (main.c:1203-1218): num sub-images of w*h RGBA floats in

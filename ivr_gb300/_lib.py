@@ -140,6 +140,8 @@ SIGNATURES = {
     "ivr_batch_set_variant": (_I, [_P, _I]),
     "ivr_device_alloc": (_I, [_P, ctypes.c_size_t, ctypes.POINTER(_P)]),
     "ivr_device_free": (_I, [_P, _P, ctypes.c_size_t]),
+    "ivr_host_alloc": (_I, [_P, ctypes.c_size_t, ctypes.POINTER(_P)]),
+    "ivr_host_free": (_I, [_P, _P]),
     "ivr_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
     "ivr_server_create": (_I, [_P, ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),
     "ivr_server_destroy": (_I, [_P]),
@@ -168,6 +170,7 @@ SIGNATURES = {
     "ivr_volume_set_mlp": (_I, [_P, _P, _F, _I]),
     "ivr_view_judge_stats": (_I, [_P, ctypes.POINTER(JudgeStats)]),
     "ivr_volume_learned_stats": (_I, [_P, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "ivr_sample_peak": (_I, [_P, _I, ctypes.POINTER(ctypes.c_double), _P]),
     "ivr_composite": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "ivr_quantize": (_I, [_P, _P, _P, ctypes.c_longlong, _P]),
 }

@@ -85,6 +85,18 @@ class Context:
         self.check(self.lib.ivr_mem_used(self.h, ctypes.byref(v)))
         return v.value
 
+    def host_frame(self, vh: int, vw: int) -> np.ndarray:
+        """A (vh, vw, 4) uint8 frame in page-locked host memory (ivr_host_alloc),
+        freed when the array is collected."""
+        p = ctypes.c_void_p()
+        n = vh * vw * 4
+        self.check(self.lib.ivr_host_alloc(self.h, n, ctypes.byref(p)))
+        buf = (ctypes.c_uint8 * n).from_address(p.value)
+        arr = np.frombuffer(buf, dtype=np.uint8).reshape(vh, vw, 4)
+        import weakref
+        weakref.finalize(buf, self.lib.ivr_host_free, None, p.value)
+        return arr
+
     def load_volume(self, vol: np.ndarray, byteswap: bool = False) -> "Volume":
         """readvoldata: a (d, h, w) uint8/uint16/float32 array to the device."""
         vol = np.ascontiguousarray(vol)
@@ -127,6 +139,12 @@ class Context:
     def composite(self, tilebuf, rcolorbuf, num: int, w: int, h: int, stream=None):
         """compositetiles: num w*h RGBA sub-images (near -> far) over tilebuf."""
         self.check(self.lib.ivr_composite(self.h, _vp(tilebuf), _vp(rcolorbuf), num, w, h, _vp(stream)))
+
+    def sample_peak(self, dtype: int, stream=None) -> float:
+        """Sample-rate roofline of the march's sampler (Gsamples/s)."""
+        g = ctypes.c_double()
+        self.check(self.lib.ivr_sample_peak(self.h, dtype, ctypes.byref(g), _vp(stream)))
+        return g.value
 
     def quantize(self, src, dst, n: int, stream=None):
         self.check(self.lib.ivr_quantize(self.h, _vp(src), _vp(dst), n, _vp(stream)))

@@ -478,6 +478,27 @@ int ivr_device_free(ivr_ctx *c, void *ptr, size_t bytes)
     return IVR_OK;
 }
 
+int ivr_host_alloc(ivr_ctx *c, size_t bytes, void **ptr)
+{
+    if (!c || !ptr || bytes == 0) return c ? fail(c, IVR_ERR_INVALID, "bad host allocation") : IVR_ERR_INVALID;
+    *ptr = nullptr;
+    CK(c, cudaSetDevice(c->device));
+    if (cudaHostAlloc(ptr, bytes, cudaHostAllocPortable) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return fail(c, IVR_ERR_NOMEM, "cudaHostAlloc(%zu) failed", bytes);
+    }
+    return IVR_OK;
+}
+
+int ivr_host_free(ivr_ctx *c, void *ptr)
+{
+    if (!ptr) return IVR_OK;
+    const cudaError_t e = cudaFreeHost(ptr);
+    if (e != cudaSuccess) return c ? cuda_fail(c, e, "cudaFreeHost") : IVR_ERR_CUDA;
+    return IVR_OK;
+}
+
 int ivr_volume_load(ivr_ctx *c, const void *host, int w, int h, int d, int dtype, int byteswap, ivr_volume **out)
 {
     if (!c || !out) return IVR_ERR_INVALID;
@@ -1044,6 +1065,68 @@ int ivr_batch_set_variant(ivr_batch *b, int variant)
     if (variant < 0 || variant >= kBatchVariants) return fail(b->ctx, IVR_ERR_INVALID, "variant %d", variant);
     b->variant = variant;
     return IVR_OK;
+}
+
+int ivr_sample_peak(ivr_ctx *c, int dtype, double *gsamples_per_s, void *stream)
+{
+    if (!c || !gsamples_per_s) return c ? fail(c, IVR_ERR_INVALID, "null output") : IVR_ERR_INVALID;
+    if (dtype < IVR_U8 || dtype > IVR_F32) return fail(c, IVR_ERR_INVALID, "unknown dtype %d", dtype);
+    cudaStream_t s = (cudaStream_t) stream;
+    // a 64^3 brick of pseudo-random values over the LUT's range, a 256-entry
+    // ramp LUT, world units = voxels
+    const int n = 64;
+    const size_t nvox = (size_t) n * n * n, esz = dtype_size(dtype);
+    std::vector<unsigned char> host(nvox * esz);
+    unsigned r = 12345u;
+    for (size_t i = 0; i < nvox; i++) {
+        r = r * 1664525u + 1013904223u;
+        const float v = (float) (r >> 8) / 16777216.0f;
+        if (dtype == IVR_U8) host[i] = (unsigned char) (v * 255.0f);
+        else if (dtype == IVR_U16) { const uint16_t u = (uint16_t) (v * 65535.0f); memcpy(&host[2 * i], &u, 2); }
+        else { const float f = v * 255.0f; memcpy(&host[4 * i], &f, 4); }
+    }
+    std::vector<float4> lut(256);
+    for (int i = 0; i < 256; i++) lut[i] = make_float4(i / 255.0f, 0.5f, 1.0f - i / 255.0f, 0.02f * (i / 255.0f));
+    const int threads = sample_peak_threads();
+    void *d_vol = nullptr, *d_lut = nullptr, *d_out = nullptr;
+    int rc = dev_alloc(c, nvox * esz, &d_vol);
+    if (rc == IVR_OK) rc = dev_alloc(c, sizeof(float4) * 256, &d_lut);
+    if (rc == IVR_OK) rc = dev_alloc(c, sizeof(float4) * (size_t) threads, &d_out);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (rc == IVR_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+        rc = fail(c, IVR_ERR_CUDA, "events");
+    if (rc == IVR_OK) {
+        FrameDesc f{};
+        f.dtype = dtype;
+        f.nb = 1;
+        f.alpha = 1.0f;
+        f.lut = (const float4 *) d_lut;
+        f.lut_n = 256;
+        f.lut_scale = dtype == IVR_U16 ? 256.0f / 65536.0f : 1.0f;
+        DevBrick &b = f.b[0];
+        b.data = d_vol;
+        b.nx = b.ny = b.nz = n;
+        b.icx = b.icy = b.icz = 1.0f;
+        const int steps = 4096;
+        long long samples = 0;
+        float ms = 0.0f;
+        cudaError_t e = cudaMemcpy(d_vol, host.data(), host.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(d_lut, lut.data(), sizeof(float4) * 256, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launch_sample_peak(f, steps, (float4 *) d_out, &samples, s);  // warm-up
+        if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+        if (e == cudaSuccess) e = launch_sample_peak(f, steps, (float4 *) d_out, &samples, s);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "sample-rate roofline");
+        else *gsamples_per_s = (double) samples / (ms * 1e-3) / 1e9;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    dev_free(c, d_vol, nvox * esz);
+    dev_free(c, d_lut, sizeof(float4) * 256);
+    dev_free(c, d_out, sizeof(float4) * (size_t) threads);
+    return rc;
 }
 
 int ivr_composite(ivr_ctx *c, float *tilebuf, const float *rcolorbuf, int num, int w, int h, void *stream)

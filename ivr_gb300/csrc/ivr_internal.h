@@ -149,6 +149,11 @@ cudaError_t noalloc_histogram(const void *data, int dtype, long long n, int hsiz
 // *tickets: how many tile tickets the launch takes from f.tickets (a
 // persistent CONFIG launch takes each tile once and each warp fails once).
 cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s, long long *tickets);
+// the sampler alone on brick f.b[0] (sample-rate roofline): every thread
+// takes `steps` samples; *samples = threads * steps; out holds one float4 per
+// thread (sample_peak_threads())
+cudaError_t launch_sample_peak(const FrameDesc &f, int steps, float4 *out, long long *samples, cudaStream_t s);
+int sample_peak_threads();
 // transparent-radius relaxation of a flag grid (kDistCap or 0 per cell)
 cudaError_t launch_dist_relax(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s);
 // batched CONFIG frames of one volume dtype; *ticket must be zero at launch

@@ -621,6 +621,50 @@ __global__ void __launch_bounds__(kThreads, JUDGE ? kJudgeBlocksPerSm : kCfgBloc
     if (CENSUS) count_exec(f, nexec, nlat);
 }
 
+// Sample-rate roofline: the CONFIG sampler (trilinear reconstruction, LUT
+// fetch, front-to-back blend) with nothing else -- no ray set-up, skipping,
+// termination or divergence -- over a brick small enough to stay in L1/L2.
+// Each thread marches its own ray of `steps` samples, 0.5 voxel apart, from
+// a start that neighbouring lanes share up to a voxel, as in an 8x4 tile.
+template <int DT>
+__global__ void __launch_bounds__(kThreads, kCfgBlocksPerSm) sample_peak_kernel(const __grid_constant__ FrameDesc f,
+                                                                                int steps, float4 *out)
+{
+    const DevBrick &b = f.b[0];
+    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
+    // the warp's 8x4 tile of starts, one voxel apart, at a hashed place
+    const unsigned w = gid >> 5, lane = gid & 31;
+    const unsigned h = w * 2654435761u;
+    const float sx = (float) (b.nx - 2), sy = (float) (b.ny - 2), sz = (float) (b.nz - 2);
+    float x = b.bminx + (2.0f + (float) (h % 997u) / 997.0f * (sx - 12.0f) + (float) (lane & 7)) / b.icx;
+    float y = b.bminy + (2.0f + (float) ((h >> 10) % 991u) / 991.0f * (sy - 8.0f) + (float) (lane >> 3)) / b.icy;
+    float z = b.bminz + (2.0f + (float) ((h >> 20) % 983u) / 983.0f * (sz - 4.0f)) / b.icz;
+    // half a voxel per step along a direction fixed per warp
+    const float dx = ((w & 1) ? 0.3f : -0.3f) / b.icx, dy = ((w & 2) ? 0.2f : -0.2f) / b.icy,
+                dz = ((w & 4) ? 0.35f : -0.35f) / b.icz;
+    const float lox = b.bminx + 1.0f / b.icx, hix = b.bminx + (sx - 1.0f) / b.icx;
+    const float loy = b.bminy + 1.0f / b.icy, hiy = b.bminy + (sy - 1.0f) / b.icy;
+    const float loz = b.bminz + 1.0f / b.icz, hiz = b.bminz + (sz - 1.0f) / b.icz;
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int i = 0; i < steps; i++) {
+        const float s = sample_cfg<DT>(b, x, y, z);
+        const float4 e = lut_at(f, (int) (s * f.lut_scale) - f.lut_off);
+        const float wgt = (1.0f - acc.w) * (e.w * f.alpha);
+        acc.x = fmaf(wgt, e.x, acc.x);
+        acc.y = fmaf(wgt, e.y, acc.y);
+        acc.z = fmaf(wgt, e.z, acc.z);
+        acc.w = acc.w * 0.5f + wgt;  // stays below 1: no termination
+        x += dx;
+        y += dy;
+        z += dz;
+        // reflect at the faces so the ray stays inside the brick
+        x = x < lox ? 2.0f * lox - x : (x > hix ? 2.0f * hix - x : x);
+        y = y < loy ? 2.0f * loy - y : (y > hiy ? 2.0f * hiy - y : y);
+        z = z < loz ? 2.0f * loz - z : (z > hiz ? 2.0f * hiz - z : z);
+    }
+    out[gid] = acc;
+}
+
 template <typename K>
 int persistent_grid(K kernel, size_t smem)
 {
@@ -739,6 +783,33 @@ cudaError_t launch_batch(int dtype, int variant, const BatchHeader *hdr, const B
     case IVR_F32: return launch_batch_dt<IVR_F32>(variant, hdr, items, ticket, s);
     default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_sample_peak(const FrameDesc &f, int steps, float4 *out, long long *samples, cudaStream_t s)
+{
+    int blocks = 0;
+    switch (f.dtype) {
+    case IVR_U8:
+        blocks = persistent_grid(sample_peak_kernel<IVR_U8>, 0);
+        sample_peak_kernel<IVR_U8><<<blocks, kThreads, 0, s>>>(f, steps, out);
+        break;
+    case IVR_U16:
+        blocks = persistent_grid(sample_peak_kernel<IVR_U16>, 0);
+        sample_peak_kernel<IVR_U16><<<blocks, kThreads, 0, s>>>(f, steps, out);
+        break;
+    case IVR_F32:
+        blocks = persistent_grid(sample_peak_kernel<IVR_F32>, 0);
+        sample_peak_kernel<IVR_F32><<<blocks, kThreads, 0, s>>>(f, steps, out);
+        break;
+    default: return cudaErrorInvalidValue;
+    }
+    *samples = (long long) blocks * kThreads * steps;
+    return cudaGetLastError();
+}
+
+int sample_peak_threads()
+{
+    return persistent_grid(sample_peak_kernel<IVR_F32>, 0) * kThreads;
 }
 
 cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s, long long *warps)

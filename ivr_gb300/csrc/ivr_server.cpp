@@ -53,6 +53,7 @@ struct Req {
     double t_submit;
     int vw, vh;
     size_t bytes;
+    bool direct;  // the output buffer is page-locked: the frame is copied straight into it
     std::shared_ptr<std::promise<int>> notify;  // front-end requests
     ivr_completion c;
 };
@@ -147,7 +148,7 @@ void finish_slot(ivr_server *s, Slot &sl)
     if (cudaEventElapsedTime(&ms, sl.t0, sl.t1) == cudaSuccess) s->gpu_s += ms / 1000.0;
     for (size_t i = 0; i < sl.reqs.size(); i++) {
         Req &q = sl.reqs[i];
-        memcpy(q.r.rgba8_host, (char *) sl.pinned + sl.offs[i], q.bytes);
+        if (!q.direct) memcpy(q.r.rgba8_host, (char *) sl.pinned + sl.offs[i], q.bytes);
         complete(s, q, IVR_OK, sl.t_start);
     }
     sl.reqs.clear();
@@ -257,8 +258,24 @@ bool dispatch(ivr_server *s, Slot &sl)
     cudaEventRecord(sl.t0, sl.stream);
     int rc = ivr_batch_render(b, 1, sl.stream);
     if (rc == IVR_OK) cudaEventRecord(sl.t1, sl.stream);
-    if (rc == IVR_OK && cudaMemcpyAsync(sl.pinned, sl.arena, off, cudaMemcpyDeviceToHost, sl.stream) != cudaSuccess)
-        rc = IVR_ERR_CUDA;
+    // frames for page-locked buffers go straight there; the others through
+    // the slot's staging, one copy per run of consecutive staged frames
+    for (size_t i = 0; i < ok.size() && rc == IVR_OK;) {
+        const size_t o = sl.offs[i];
+        if (ok[i].direct) {
+            if (cudaMemcpyAsync(ok[i].r.rgba8_host, (char *) sl.arena + o, ok[i].bytes, cudaMemcpyDeviceToHost,
+                                sl.stream) != cudaSuccess)
+                rc = IVR_ERR_CUDA;
+            i++;
+            continue;
+        }
+        size_t j = i, end = o;
+        while (j < ok.size() && !ok[j].direct) end = sl.offs[j] + ok[j].bytes, j++;
+        if (cudaMemcpyAsync((char *) sl.pinned + o, (char *) sl.arena + o, end - o, cudaMemcpyDeviceToHost,
+                            sl.stream) != cudaSuccess)
+            rc = IVR_ERR_CUDA;
+        i = j;
+    }
     if (rc == IVR_OK && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) rc = IVR_ERR_CUDA;
     if (rc != IVR_OK) {
         for (auto &q : ok) complete(s, q, rc, sl.t_start);
@@ -321,6 +338,21 @@ void scheduler(ivr_server *s)
     }
 }
 
+// Both ends of [p, p + n) in page-locked host memory (cudaHostAlloc or
+// cudaHostRegister): the device can copy into it directly.
+bool page_locked(const void *p, size_t n)
+{
+    for (const char *q : {(const char *) p, (const char *) p + n - 1}) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost) return false;
+    }
+    return true;
+}
+
 int submit_req(ivr_server *s, const ivr_request *r, std::shared_ptr<std::promise<int>> notify)
 {
     if (r->volume < 0 || r->volume >= (int) s->vols.size()) return IVR_ERR_INVALID;
@@ -332,6 +364,7 @@ int submit_req(ivr_server *s, const ivr_request *r, std::shared_ptr<std::promise
     q.vh = viewport_dim(r->state.winheight, s->params.tileh);
     if (q.vw < 1 || q.vh < 1) return IVR_ERR_INVALID;
     q.bytes = (size_t) q.vw * q.vh * 4;
+    q.direct = page_locked(r->rgba8_host, q.bytes);
     q.notify = std::move(notify);
     memset(&q.c, 0, sizeof(q.c));
     {

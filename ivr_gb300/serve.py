@@ -38,12 +38,30 @@ def schedule(clients=32, rate=(10.0, 60.0), duration=5.0, seed=0):
 def run(server, volumes, scales, duration=5.0, clients=32, rate=(10.0, 60.0), sizes=SIZES, seed=0,
         tf_every=5, keep_frames=False):
     """Drives `server` (ivr_gb300.api.Server) for `duration` seconds.
-    volumes: server volume ids; scales: LUT scale per volume.  Returns the
-    completions and the wall time."""
+    volumes: server volume ids; scales: LUT scale per volume.  Frames land in
+    a pool of page-locked buffers that is reused as requests complete (as a
+    client reuses its frame buffer).  Returns the completions and the wall
+    time."""
     rng = np.random.default_rng(seed + 1)
     events = schedule(clients, rate, duration, seed)
     client_tf = {}
     sent = {}
+    # (vh, vw) -> free page-locked frames, kept on the server so that runs
+    # after a warm-up one find their buffers allocated
+    pool = server.__dict__.setdefault("_frame_pool", {})
+
+    def frame_for(w, h):
+        free = pool.setdefault((h, w), [])
+        return free.pop() if free else server.ctx.host_frame(h, w)
+
+    def collect(got):
+        for r in got:
+            f = r.get("frame")
+            if f is not None:
+                if keep_frames:
+                    r["frame"] = f.copy()
+                pool.setdefault(f.shape[:2], []).append(f)
+            done.append(r)
     for c in range(clients):  # every client starts with its own TF per volume scale
         client_tf[c] = {s: server.add_tf(synth.knot_tf(seed * 1000 + c)[0], 0, s) for s in set(scales)}
     count = {c: 0 for c in range(clients)}
@@ -61,21 +79,21 @@ def run(server, volumes, scales, duration=5.0, clients=32, rate=(10.0, 60.0), si
         if now < t_arr:
             time.sleep(t_arr - now)
         late = max(0.0, time.perf_counter() - t0 - t_arr)
-        server.submit(volumes[vi], client_tf[c][scales[vi]], st, tag)
+        server.submit(volumes[vi], client_tf[c][scales[vi]], st, tag, out=frame_for(w, h))
         sent[tag] = (late, vi, (w, h), st, client_tf[c][scales[vi]])
-        for r in server.poll(wait_ms=0):
-            done.append(r)
+        collect(server.poll(wait_ms=0))
     while len(done) < len(events):
         got = server.poll(wait_ms=50)
         if not got and time.perf_counter() - t0 > duration + 60:
             break
-        done.extend(got)
+        collect(got)
     wall = time.perf_counter() - t0
     out = []
     for r in done:
         late, vi, size, st, tf = sent[r["tag"]]
         r = dict(r)
         r["latency"] = r["t_total"] + late
+        r["late"] = late
         r["volume"], r["size"], r["state"], r["tf"] = vi, size, st, tf
         if not keep_frames:
             r.pop("frame", None)

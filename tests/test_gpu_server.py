@@ -40,7 +40,10 @@ def vols(gpu_lib):
     ctx.close()
 
 
-def test_served_frames_equal_frames_rendered_alone(vols):
+@pytest.mark.parametrize("pinned", [False, True], ids=["staged", "page-locked"])
+def test_served_frames_equal_frames_rendered_alone(vols, pinned):
+    """Pageable output buffers go through the server's staging copy;
+    page-locked ones (ivr_host_alloc) receive the frame directly."""
     ctx, vs = vols
     srv = api.Server(ctx, slots=3, max_batch_frames=8, arena_mib=8)
     ids = [srv.add_volume(v) for v, _ in vs]
@@ -52,7 +55,8 @@ def test_served_frames_equal_frames_rendered_alone(vols):
         k, t = int(rng.integers(3)), int(rng.integers(3))
         w, h = [(48, 48), (64, 40), (80, 80), (32, 56)][tag % 4]
         st = orbit_state(float(rng.uniform(0, 360)), float(rng.uniform(-50, 50)), w, h, fovy=30.0, alpha=1.0)
-        srv.submit(ids[k], tf_ids[(t, k)], st, tag)
+        out = ctx.host_frame(h, w) if pinned else None
+        srv.submit(ids[k], tf_ids[(t, k)], st, tag, out=out)
         reqs[tag] = (k, t, st)
     done = []
     while len(done) < len(reqs):
