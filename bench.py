@@ -557,6 +557,23 @@ def main():
     sp = stream.cuda_stream
     o8 = torch.empty((h, w, 4), dtype=torch.uint8, device="cuda")
 
+    # the plain march (no skipping) on the first views: its executed
+    # samples/s against the sample-rate roofline (outside the timed region)
+    plain_view = ctx.view()
+    plain_params = api.config_params(step=wl["step"], term_alpha=wl["term"], skip=False)
+    p_exec, p_ms = 0, 0.0
+    for st in states[args.warmup:args.warmup + 3]:
+        plain_view.set(v, st, plain_params)
+        p_exec += plain_view.census(tf, sp)["executed"]
+        plain_view.render(tf, None, o8.data_ptr(), sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plain_view.render(tf, None, o8.data_ptr(), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        p_ms += e0.elapsed_time(e1)
+    plain_view.free()
+
     # work census of the timed views (diagnostic launches, outside timing)
     lattice = executed = touched = 0
     for st in states[args.warmup:]:
@@ -643,6 +660,10 @@ def main():
                                 "frac": executed / args.steps / (kavg / 1000.0) / 1e9 / sample_peak,
                                 "note": "executed samples/s of the render launch against ivr_sample_peak: the "
                                         "same sampler, LUT fetch and blend alone on a cache-resident brick"},
+            "plain_kernel": {"executed_gsamples_per_s": p_exec / (p_ms / 1000.0) / 1e9,
+                             "frac_of_sample_roofline": p_exec / (p_ms / 1000.0) / 1e9 / sample_peak,
+                             "ms_per_frame": p_ms / 3,
+                             "note": "the march without skipping (the plain method) on 3 of the views"},
             "gpu_launches": args.steps,
             "clocks": clk.summary(),
         }

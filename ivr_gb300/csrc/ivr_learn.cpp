@@ -381,19 +381,35 @@ int ivr_mlp_add_samples(ivr_mlp *m, ivr_volume *v, ivr_tf *tf, long long *total)
     const long long cells = volume_cells(v);
     if (m->n + cells > (long long) 0x7fffffff) return fail(c, IVR_ERR_INVALID, "training set above 2^31 rows");
     CK(c, cudaDeviceSynchronize());
-    long long cap = m->cap;
-    rc = grow(c, (void **) &m->d_X, &cap, m->n + cells, kMlpIn * kBf16Bytes, m->n);
-    if (rc) return rc;
-    long long cap2 = m->cap;
-    rc = grow(c, (void **) &m->d_T, &cap2, m->n + cells, sizeof(float), m->n);
-    if (rc) return rc;
-    long long cap3 = m->cap;
-    rc = grow(c, (void **) &m->d_Y, &cap3, m->n + cells, sizeof(float), 0);
-    if (rc) return rc;
-    long long cap4 = m->cap;
-    rc = grow(c, (void **) &m->d_idx, &cap4, m->n + cells, sizeof(int), 0);
-    if (rc) return rc;
-    m->cap = cap;
+    if (m->n + cells > m->cap) {
+        // all four arrays move to the new capacity together, or none does
+        const long long nc = std::max(m->n + cells, m->cap * 2);
+        void *x = nullptr, *t = nullptr, *y = nullptr, *ix = nullptr;
+        rc = dev_alloc(c, (size_t) nc * kMlpIn * kBf16Bytes, &x);
+        if (rc == IVR_OK) rc = dev_alloc(c, (size_t) nc * sizeof(float), &t);
+        if (rc == IVR_OK) rc = dev_alloc(c, (size_t) nc * sizeof(float), &y);
+        if (rc == IVR_OK) rc = dev_alloc(c, (size_t) nc * sizeof(int), &ix);
+        if (rc == IVR_OK && m->n > 0 &&
+            (cudaMemcpy(x, m->d_X, (size_t) m->n * kMlpIn * kBf16Bytes, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+             cudaMemcpy(t, m->d_T, (size_t) m->n * sizeof(float), cudaMemcpyDeviceToDevice) != cudaSuccess))
+            rc = fail(c, IVR_ERR_CUDA, "copying the training set");
+        if (rc) {
+            dev_free(c, x, (size_t) nc * kMlpIn * kBf16Bytes);
+            dev_free(c, t, (size_t) nc * sizeof(float));
+            dev_free(c, y, (size_t) nc * sizeof(float));
+            dev_free(c, ix, (size_t) nc * sizeof(int));
+            return rc;
+        }
+        dev_free(c, m->d_X, (size_t) m->cap * kMlpIn * kBf16Bytes);
+        dev_free(c, m->d_T, (size_t) m->cap * sizeof(float));
+        dev_free(c, m->d_Y, (size_t) m->cap * sizeof(float));
+        dev_free(c, m->d_idx, (size_t) m->cap * sizeof(int));
+        m->d_X = (uint16_t *) x;
+        m->d_T = (float *) t;
+        m->d_Y = (float *) y;
+        m->d_idx = (int *) ix;
+        m->cap = nc;
+    }
     rc = features(m, v, tf, m->d_X + m->n * kMlpIn, m->d_T + m->n, 0);
     if (rc) return rc;
     CK(c, cudaDeviceSynchronize());

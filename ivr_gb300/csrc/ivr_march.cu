@@ -42,12 +42,6 @@ __device__ __forceinline__ float vload(const void *p, long long i)
 {
     return (float) __ldg(reinterpret_cast<const typename VoxT<DT>::T *>(p) + i);
 }
-// bricks hold fewer than 2^32 voxels (checked at load), so 32-bit offsets
-template <int DT>
-__device__ __forceinline__ float vload32(const void *p, unsigned i)
-{
-    return (float) __ldg(reinterpret_cast<const typename VoxT<DT>::T *>(p) + i);
-}
 
 // getrayintersect (ray.c:276-318).  All six planes are visited: once
 // tin >= tout no later plane can make it a hit, so skipping the reference's
@@ -144,18 +138,28 @@ __device__ __forceinline__ float sample_cfg(const DevBrick &b, float x, float y,
     float ux = (x - b.bminx) * b.icx;
     float uy = (y - b.bminy) * b.icy;
     float uz = (z - b.bminz) * b.icz;
-    int j = min(max(__float2int_rd(ux), 0), nx - 2);
-    int i = min(max(__float2int_rd(uy), 0), ny - 2);
-    int k = min(max(__float2int_rd(uz), 0), nz - 2);
-    float fx = fminf(fmaxf(ux - (float) j, 0.0f), 1.0f);
-    float fy = fminf(fmaxf(uy - (float) i, 0.0f), 1.0f);
-    float fz = fminf(fmaxf(uz - (float) k, 0.0f), 1.0f);
-    const unsigned sy = (unsigned) nx, sz = (unsigned) nx * (unsigned) ny;
-    const unsigned p = (unsigned) k * sz + (unsigned) i * sy + (unsigned) j;
-    float c00 = lerpf(vload32<DT>(b.data, p), vload32<DT>(b.data, p + 1), fx);
-    float c10 = lerpf(vload32<DT>(b.data, p + sy), vload32<DT>(b.data, p + sy + 1), fx);
-    float c01 = lerpf(vload32<DT>(b.data, p + sz), vload32<DT>(b.data, p + sz + 1), fx);
-    float c11 = lerpf(vload32<DT>(b.data, p + sz + sy), vload32<DT>(b.data, p + sz + sy + 1), fx);
+    // clamp to edge: the coordinate to [0, n-1], the cell to [0, n-2]; then
+    // the fraction u - floor(u) is exact and lies in [0, 1] (this gives the
+    // same cell and fraction as clamping the cell and then the fraction)
+    ux = fminf(fmaxf(ux, 0.0f), (float) (nx - 1));
+    uy = fminf(fmaxf(uy, 0.0f), (float) (ny - 1));
+    uz = fminf(fmaxf(uz, 0.0f), (float) (nz - 1));
+    const int j = min(__float2int_rd(ux), nx - 2);
+    const int i = min(__float2int_rd(uy), ny - 2);
+    const int k = min(__float2int_rd(uz), nz - 2);
+    const float fx = ux - (float) j, fy = uy - (float) i, fz = uz - (float) k;
+    // one pointer to the cell's low corner (a brick holds fewer than 2^32
+    // voxels, checked at load, so its offset fits 32 bits); the other
+    // corners are whole rows (nx) and slabs (nx*ny) away, the +1 neighbours
+    // an immediate offset
+    using T = typename VoxT<DT>::T;
+    const unsigned sz = (unsigned) nx * (unsigned) ny;
+    const T *q0 = reinterpret_cast<const T *>(b.data) + ((unsigned) k * sz + (unsigned) i * (unsigned) nx + (unsigned) j);
+    const T *q1 = q0 + nx, *q2 = q0 + sz, *q3 = q2 + nx;
+    float c00 = lerpf((float) __ldg(q0), (float) __ldg(q0 + 1), fx);
+    float c10 = lerpf((float) __ldg(q1), (float) __ldg(q1 + 1), fx);
+    float c01 = lerpf((float) __ldg(q2), (float) __ldg(q2 + 1), fx);
+    float c11 = lerpf((float) __ldg(q3), (float) __ldg(q3 + 1), fx);
     float c0 = lerpf(c00, c10, fy);
     float c1 = lerpf(c01, c11, fy);
     return lerpf(c0, c1, fz);
