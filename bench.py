@@ -59,7 +59,7 @@ BATCH = dict(base="sorted_brick_512", views=64, tfs=4, sizes=[(256, 256), (512, 
 SERVE = dict(volumes=[((256, 256, 256), "u8", 8, 0.05, 0.0, 0.0), ((512, 512, 512), "u16", 64, 0.0, 0.0, 0.0),
                       ((512, 512, 512), "f32", 64, 0.0, 0.1, 0.0), ((1024, 1024, 1024), "u16", 256, 0.0, 0.0, 0.7)],
              clients=32, rate=(10.0, 60.0), duration=10.0, warm=2.0, slots=4, batch=16, arena_mib=160,
-             budget_gib=12)
+             budget_gib=32)
 # learned empty-space skipping: 1024^3 u16 of 256 blobs (sigmas scaled by
 # (8/256)^(1/3) so they do not sum to saturation) with 70% of the
 # macrocells exactly zero, 1920x1080, 50 random 16-knot TFs (the lowest
@@ -245,6 +245,7 @@ def config_of(args, wl):
     return {"workload": args.workload, "volume": "x".join(map(str, wl["shape"][::-1])) + " " + wl["dtype"],
             "bricks": "x".join(map(str, wl["bricks"])) + " + 1-voxel halo", "image": f"{w}x{h}",
             "step_voxels": wl["step"], "early_termination_alpha": wl["term"], "skip": "16^3 macrocell grid",
+            "layout": "bricks" if args.linear else "bricks + corner-packed copies",
             "tf": "256-entry RGBA FP32 ramp", "l2": "inputs larger than L2 (volume resident, > 129 MB)",
             "parallelism": f"replicas x{args.gpus}"}
 
@@ -516,6 +517,8 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=0)
     ap.add_argument("--serve-batch", type=int, default=0)
     ap.add_argument("--serve-rate", default="", help="per-client request rate range lo,hi (req/s)")
+    ap.add_argument("--linear", action="store_true",
+                    help="render from the bricks themselves, without the corner-packed copies")
     ap.add_argument("--no-extras", action="store_true",
                     help="default workload only: skip the learned-skip and serving summaries")
     args = ap.parse_args()
@@ -549,7 +552,7 @@ def main():
     lut = synth.ramp_tf(256)
 
     ctx = api.Context(local)
-    v = ctx.load_volume(vol).bricks(*wl["bricks"], overlap=1)
+    v = ctx.load_volume(vol).bricks(*wl["bricks"], overlap=1).quads(not args.linear)
     tf = ctx.transfer_function().set_lut(lut, 0, lut_scale(wl), api.TF_F2B)
     params = api.config_params(step=wl["step"], term_alpha=wl["term"], skip=True)
     view = ctx.view()

@@ -153,6 +153,15 @@ int ivr_volume_free(ivr_volume *vol);
  * (getlocalbrick).  Each brick becomes its own device array.  The default
  * after load is one brick. */
 int ivr_bricks_setup(ivr_volume *vol, int py, int px, int pz, int overlap);
+/* Corner-packed brick copies (no counterpart in the reference; on by
+ * default).  Each brick gets a second copy in which element (j, i, k) holds
+ * the four voxels (j, i), (j+1, i), (j, i+1), (j+1, i+1) of slab k, so a
+ * trilinear sample of the CONFIG march is two vector loads instead of eight
+ * gathers.  It costs 4x the brick's bytes of HBM; a copy that does not fit
+ * the budget is left out and the march reads the brick itself.  The images
+ * are the same either way.  Switching rebuilds the bricks. */
+int ivr_volume_set_quads(ivr_volume *vol, int on);
+int ivr_volume_quad_bytes(const ivr_volume *vol, size_t *bytes);  /* bytes held by the copies */
 /* min, max and the histogram of mathutil.c:444-470 (hist may be NULL;
  * otherwise it holds hsize = (int)(max-min+1) bins). */
 int ivr_volume_minmax(ivr_volume *vol, float *mn, float *mx);
@@ -372,10 +381,11 @@ int ivr_view_judge_stats(ivr_view *view, ivr_judge_stats *stats);
 
 /* --- measurement -------------------------------------------------------- */
 /* The sample-rate roofline of the CONFIG march (no counterpart in the
- * reference): the sampler alone -- trilinear reconstruction, LUT fetch,
- * front-to-back blend, no ray set-up, skipping or divergence -- on a 64^3
- * brick of `dtype` that stays in cache, every resident thread marching its
- * own ray.  Samples per second / 1e9 (waits for the timing). */
+ * reference): the sampler alone -- trilinear reconstruction from the
+ * corner-packed layout, LUT fetch, front-to-back blend, no ray set-up,
+ * skipping or divergence -- on a 64^3 brick of `dtype` that stays in cache,
+ * every resident thread marching its own ray.  Samples per second / 1e9
+ * (waits for the timing). */
 int ivr_sample_peak(ivr_ctx *ctx, int dtype, double *gsamples_per_s, void *stream);
 
 /* --- compositing and output -------------------------------------------- */

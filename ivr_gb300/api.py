@@ -159,6 +159,16 @@ class Volume:
         self.ctx.check(self.ctx.lib.ivr_bricks_setup(self.h, py, px, pz, overlap))
         return self
 
+    def quads(self, on: bool) -> "Volume":
+        """Corner-packed brick copies on/off (on by default)."""
+        self.ctx.check(self.ctx.lib.ivr_volume_set_quads(self.h, int(on)))
+        return self
+
+    def quad_bytes(self) -> int:
+        n = ctypes.c_size_t()
+        self.ctx.check(self.ctx.lib.ivr_volume_quad_bytes(self.h, ctypes.byref(n)))
+        return n.value
+
     def minmax(self):
         mn, mx = ctypes.c_float(), ctypes.c_float()
         self.ctx.check(self.ctx.lib.ivr_volume_minmax(self.h, ctypes.byref(mn), ctypes.byref(mx)))

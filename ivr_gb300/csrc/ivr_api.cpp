@@ -107,6 +107,7 @@ void free_bricks(ivr_volume *v)
     for (auto &b : v->bricks) {
         if (b.owns) dev_free(v->ctx, b.data, brick_bytes(v, b));
         dev_free(v->ctx, b.mc_minmax, mc_cells(b) * 2 * sizeof(float));
+        if (b.quad) dev_free(v->ctx, b.quad, quad_bytes(v->dtype, b.lw, b.lh, b.ld));
     }
     v->bricks.clear();
 }
@@ -149,6 +150,16 @@ int setup_bricks(ivr_volume *v, int py, int px, int pz, int overlap)
         }
         int rc = build_macrocells(v, b);
         if (rc) { free_bricks(v); return rc; }
+        if (v->quads) {
+            // the corner-packed copy is an accelerator: without room for it
+            // the march reads the brick itself
+            const size_t qb = quad_bytes(v->dtype, b.lw, b.lh, b.ld);
+            const std::string err = c->err;
+            if (dev_alloc(c, qb, &b.quad) == IVR_OK)
+                CK(c, launch_quads(b.data, v->dtype, b.lw, b.lh, b.ld, b.quad, 0));
+            else
+                c->err = err;
+        }
     }
     CK(c, cudaDeviceSynchronize());
     v->py = py; v->px = px; v->pz = pz; v->overlap = overlap;
@@ -561,6 +572,24 @@ int ivr_bricks_setup(ivr_volume *v, int py, int px, int pz, int overlap)
 {
     if (!v) return IVR_ERR_INVALID;
     return setup_bricks(v, py, px, pz, overlap);
+}
+
+int ivr_volume_set_quads(ivr_volume *v, int on)
+{
+    if (!v) return IVR_ERR_INVALID;
+    if (v->quads == (on != 0)) return IVR_OK;
+    v->quads = on != 0;
+    return setup_bricks(v, v->py, v->px, v->pz, v->overlap);  // rebuilt with or without the copies
+}
+
+int ivr_volume_quad_bytes(const ivr_volume *v, size_t *bytes)
+{
+    if (!v || !bytes) return IVR_ERR_INVALID;
+    size_t n = 0;
+    for (const auto &b : v->bricks)
+        if (b.quad) n += quad_bytes(v->dtype, b.lw, b.lh, b.ld);
+    *bytes = n;
+    return IVR_OK;
 }
 
 int ivr_volume_minmax(ivr_volume *v, float *mn, float *mx)
@@ -1088,8 +1117,10 @@ int ivr_sample_peak(ivr_ctx *c, int dtype, double *gsamples_per_s, void *stream)
     std::vector<float4> lut(256);
     for (int i = 0; i < 256; i++) lut[i] = make_float4(i / 255.0f, 0.5f, 1.0f - i / 255.0f, 0.02f * (i / 255.0f));
     const int threads = sample_peak_threads();
-    void *d_vol = nullptr, *d_lut = nullptr, *d_out = nullptr;
+    void *d_vol = nullptr, *d_lut = nullptr, *d_out = nullptr, *d_quad = nullptr;
+    const size_t qb = quad_bytes(dtype, n, n, n);
     int rc = dev_alloc(c, nvox * esz, &d_vol);
+    if (rc == IVR_OK) rc = dev_alloc(c, qb, &d_quad);
     if (rc == IVR_OK) rc = dev_alloc(c, sizeof(float4) * 256, &d_lut);
     if (rc == IVR_OK) rc = dev_alloc(c, sizeof(float4) * (size_t) threads, &d_out);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1105,12 +1136,14 @@ int ivr_sample_peak(ivr_ctx *c, int dtype, double *gsamples_per_s, void *stream)
         f.lut_scale = dtype == IVR_U16 ? 256.0f / 65536.0f : 1.0f;
         DevBrick &b = f.b[0];
         b.data = d_vol;
+        b.quad = d_quad;  // the layout the march reads
         b.nx = b.ny = b.nz = n;
         b.icx = b.icy = b.icz = 1.0f;
         const int steps = 4096;
         long long samples = 0;
         float ms = 0.0f;
         cudaError_t e = cudaMemcpy(d_vol, host.data(), host.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launch_quads(d_vol, dtype, n, n, n, d_quad, s);
         if (e == cudaSuccess) e = cudaMemcpy(d_lut, lut.data(), sizeof(float4) * 256, cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = launch_sample_peak(f, steps, (float4 *) d_out, &samples, s);  // warm-up
         if (e == cudaSuccess) e = cudaEventRecord(e0, s);
@@ -1124,6 +1157,7 @@ int ivr_sample_peak(ivr_ctx *c, int dtype, double *gsamples_per_s, void *stream)
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     dev_free(c, d_vol, nvox * esz);
+    dev_free(c, d_quad, qb);
     dev_free(c, d_lut, sizeof(float4) * 256);
     dev_free(c, d_out, sizeof(float4) * (size_t) threads);
     return rc;

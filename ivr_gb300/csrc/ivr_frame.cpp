@@ -186,6 +186,7 @@ int build_frame(int gw, int gh, int gd, int dtype, const HostBrick *bricks, int 
         const HostBrick &hb = bricks[k];
         DevBrick &b = f.b[k];
         b.data = hb.data;
+        b.quad = hb.quad;
         b.nx = hb.lw; b.ny = hb.lh; b.nz = hb.ld;
         b.bminx = hb.bminx; b.bminy = hb.bminy; b.bminz = hb.bminz;
         b.w = hb.w; b.h = hb.h; b.d = hb.d;

@@ -29,6 +29,7 @@ struct ivr_volume {
     size_t full_bytes = 0;
     std::vector<ivr::HostBrick> bricks;
     int py = 1, px = 1, pz = 1, overlap = 0;
+    bool quads = true;  // keep corner-packed copies of the bricks (HostBrick::quad)
     bool have_minmax = false;
     float vmin = 0.0f, vmax = 0.0f;
     // macrocell distance fields, one set per transfer function in use

@@ -30,6 +30,9 @@ struct DevBrick {
                             // (Chebyshev) is transparent; or null
     int mcx, mcy, mcz;      // macrocell grid dims
     uint8_t *touched;       // census only: cells an executed sample read
+    const void *quad;       // corner-packed copy or null: element (j, i, k),
+                            // j < nx-1, i < ny-1, holds the voxels (j, i),
+                            // (j+1, i), (j, i+1), (j+1, i+1) of slab k
 };
 
 // Learned-skip judge words of a view (device).  maxdiff and warps_done are
@@ -120,6 +123,7 @@ struct HostBrick {
     bool owns;          // false when it aliases the full volume
     float *mc_minmax;   // device [mcz][mcy][mcx][2]
     int mcx, mcy, mcz;
+    void *quad;         // device corner-packed copy (DevBrick::quad) or null
 };
 
 size_t dtype_size(int dtype);
@@ -135,6 +139,10 @@ cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int n
                               int mcz, cudaStream_t s);
 cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const int *nzprefix, int lut_n,
                                int lut_off, float lut_scale, uint8_t *empty, cudaStream_t s);
+// corner-packed copy of an nx x ny x nz brick: (nx-1)(ny-1)nz four-voxel
+// elements of 4 * sizeof(dtype) bytes
+size_t quad_bytes(int dtype, int nx, int ny, int nz);
+cudaError_t launch_quads(const void *data, int dtype, int nx, int ny, int nz, void *quad, cudaStream_t s);
 cudaError_t launch_composite(float *dst, const float *src, int num, long long npix, cudaStream_t s);
 cudaError_t launch_quantize(const float *in, uint8_t *out, long long n, cudaStream_t s);
 int minmax_parts();

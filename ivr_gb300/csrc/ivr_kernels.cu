@@ -382,6 +382,41 @@ cudaError_t launch_dist_relax(uint8_t *dist, int mcx, int mcy, int mcz, cudaStre
     return cudaGetLastError();
 }
 
+template <typename T, typename V>
+__global__ void quad_kernel(const T *src, int nx, int ny, int nz, V *dst)
+{
+    const long long qx = nx - 1, qy = ny - 1, n = qx * qy * nz;
+    for (long long e = blockIdx.x * (long long) blockDim.x + threadIdx.x; e < n;
+         e += (long long) gridDim.x * blockDim.x) {
+        const long long j = e % qx, r = e / qx, i = r % qy, k = r / qy;
+        const T *p = src + (k * ny + i) * nx + j;
+        V v;
+        v.x = p[0];
+        v.y = p[1];
+        v.z = p[nx];
+        v.w = p[nx + 1];
+        dst[e] = v;
+    }
+}
+
+size_t quad_bytes(int dtype, int nx, int ny, int nz)
+{
+    return (size_t) (nx - 1) * (ny - 1) * nz * 4 * dtype_size(dtype);
+}
+
+cudaError_t launch_quads(const void *data, int dtype, int nx, int ny, int nz, void *quad, cudaStream_t s)
+{
+    const long long n = (long long) (nx - 1) * (ny - 1) * nz;
+    const int grid = grid_for(n, 256);
+    switch (dtype) {
+    case IVR_U8: quad_kernel<<<grid, 256, 0, s>>>((const uint8_t *) data, nx, ny, nz, (uchar4 *) quad); break;
+    case IVR_U16: quad_kernel<<<grid, 256, 0, s>>>((const uint16_t *) data, nx, ny, nz, (ushort4 *) quad); break;
+    case IVR_F32: quad_kernel<<<grid, 256, 0, s>>>((const float *) data, nx, ny, nz, (float4 *) quad); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_composite(float *dst, const float *src, int num, long long npix, cudaStream_t s)
 {
     composite_kernel<<<grid_for(npix, 256), 256, 0, s>>>((float4 *) dst, (const float4 *) src, num, npix);

@@ -33,9 +33,9 @@ constexpr int kJudgeBlocksPerSm = 7;
 constexpr int kBatchBlocksPerSm = 6;
 
 template <int DT> struct VoxT;
-template <> struct VoxT<IVR_U8> { using T = uint8_t; };
-template <> struct VoxT<IVR_U16> { using T = uint16_t; };
-template <> struct VoxT<IVR_F32> { using T = float; };
+template <> struct VoxT<IVR_U8> { using T = uint8_t; using V4 = uchar4; };
+template <> struct VoxT<IVR_U16> { using T = uint16_t; using V4 = ushort4; };
+template <> struct VoxT<IVR_F32> { using T = float; using V4 = float4; };
 
 template <int DT>
 __device__ __forceinline__ float vload(const void *p, long long i)
@@ -148,18 +148,31 @@ __device__ __forceinline__ float sample_cfg(const DevBrick &b, float x, float y,
     const int i = min(__float2int_rd(uy), ny - 2);
     const int k = min(__float2int_rd(uz), nz - 2);
     const float fx = ux - (float) j, fy = uy - (float) i, fz = uz - (float) k;
-    // one pointer to the cell's low corner (a brick holds fewer than 2^32
-    // voxels, checked at load, so its offset fits 32 bits); the other
-    // corners are whole rows (nx) and slabs (nx*ny) away, the +1 neighbours
-    // an immediate offset
-    using T = typename VoxT<DT>::T;
-    const unsigned sz = (unsigned) nx * (unsigned) ny;
-    const T *q0 = reinterpret_cast<const T *>(b.data) + ((unsigned) k * sz + (unsigned) i * (unsigned) nx + (unsigned) j);
-    const T *q1 = q0 + nx, *q2 = q0 + sz, *q3 = q2 + nx;
-    float c00 = lerpf((float) __ldg(q0), (float) __ldg(q0 + 1), fx);
-    float c10 = lerpf((float) __ldg(q1), (float) __ldg(q1 + 1), fx);
-    float c01 = lerpf((float) __ldg(q2), (float) __ldg(q2 + 1), fx);
-    float c11 = lerpf((float) __ldg(q3), (float) __ldg(q3 + 1), fx);
+    float c00, c10, c01, c11;
+    if (b.quad) {
+        // corner-packed copy: the cell's 8 voxels in two vector loads
+        using V = typename VoxT<DT>::V4;
+        const unsigned qx = (unsigned) nx - 1u, qs = qx * ((unsigned) ny - 1u);
+        const V *e = reinterpret_cast<const V *>(b.quad) + ((unsigned) k * qs + (unsigned) i * qx + (unsigned) j);
+        const V lo = __ldg(e), hi = __ldg(e + qs);
+        c00 = lerpf((float) lo.x, (float) lo.y, fx);
+        c10 = lerpf((float) lo.z, (float) lo.w, fx);
+        c01 = lerpf((float) hi.x, (float) hi.y, fx);
+        c11 = lerpf((float) hi.z, (float) hi.w, fx);
+    } else {
+        // one pointer to the cell's low corner (a brick holds fewer than
+        // 2^32 voxels, checked at load, so its offset fits 32 bits); the
+        // other corners are whole rows (nx) and slabs (nx*ny) away, the +1
+        // neighbours an immediate offset
+        using T = typename VoxT<DT>::T;
+        const unsigned sz = (unsigned) nx * (unsigned) ny;
+        const T *q0 = reinterpret_cast<const T *>(b.data) + ((unsigned) k * sz + (unsigned) i * (unsigned) nx + (unsigned) j);
+        const T *q1 = q0 + nx, *q2 = q0 + sz, *q3 = q2 + nx;
+        c00 = lerpf((float) __ldg(q0), (float) __ldg(q0 + 1), fx);
+        c10 = lerpf((float) __ldg(q1), (float) __ldg(q1 + 1), fx);
+        c01 = lerpf((float) __ldg(q2), (float) __ldg(q2 + 1), fx);
+        c11 = lerpf((float) __ldg(q3), (float) __ldg(q3 + 1), fx);
+    }
     float c0 = lerpf(c00, c10, fy);
     float c1 = lerpf(c01, c11, fy);
     return lerpf(c0, c1, fz);

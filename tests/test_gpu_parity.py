@@ -167,8 +167,11 @@ def make_config_volume(shape, dtype, seed):
     return synth.blob_volume(shape, n_blobs=8, seed=seed, dtype=dtype, zero_fraction=0.5, cell=8)
 
 
+@pytest.mark.parametrize("quads", [True, False], ids=["quads", "linear"])
 @pytest.mark.parametrize("case", CONFIG_CASES, ids=[str(i) for i in range(len(CONFIG_CASES))])
-def test_config_preset_matches_o2(ctx, oracle_mod, case):
+def test_config_preset_matches_o2(ctx, oracle_mod, case, quads):
+    """Both sampler layouts (corner-packed copies and the bricks themselves)
+    give O2's frame bit for bit."""
     shape, dtype, procdims, az, el, win, step, term, skip = case
     vol = make_config_volume(shape, dtype, 7)
     lut = synth.ramp_tf(256)
@@ -176,9 +179,10 @@ def test_config_preset_matches_o2(ctx, oracle_mod, case):
     st = orbit_state(az, el, win[0], win[1], fovy=30.0, alpha=1.0)
     ref = oracle_mod.render(vol, st, lut, 0, 6, preset=1, procdims=procdims, step=step, term_alpha=term,
                             lut_scale=scale)
-    v = ctx.load_volume(vol)
+    v = ctx.load_volume(vol).quads(quads)
     if np.prod(procdims) > 1:
         v.bricks(*procdims)
+    assert (v.quad_bytes() > 0) == quads
     tf = ctx.transfer_function().set_lut(lut, 0, scale, api.TF_F2B)
     p = api.config_params(step=step, term_alpha=term, skip=skip)
     view = ctx.view().set(v, st, p)
