@@ -70,6 +70,9 @@ LEARNED = dict(shape=(1024, 1024, 1024), dtype="u16", n_blobs=256, sigma_scale=(
                zero_fraction=0.7, image=(1920, 1080),
                step=0.5, term=0.99, fovy=30.0, seed=3, tfs=50, train_tfs=8, epochs=30, batch_rows=8192, lr=2e-3,
                wneg=4.0, slack=0.02, judge_stride=16, frames=3)
+# the same at 256^3 and 1280x720 with 10 TFs: the case ncu captures
+LEARNED_SMALL = dict(LEARNED, shape=(256, 256, 256), n_blobs=32, sigma_scale=(8 / 32) ** (1 / 3), image=(1280, 720),
+                     tfs=10, train_tfs=4, epochs=5)
 METRIC = "frames/s & Gsamples/s, learned-skip vs plain GPU at <=1/255 err; p99 ms"
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "march_cfg_sorted_brick_512.txt")
 
@@ -379,7 +382,7 @@ def run_learned(args, quiet=False):
     import torch
     from ivr_gb300 import api, synth
     from ivr_gb300.state import orbit_state
-    L = LEARNED
+    L = LEARNED_SMALL if getattr(args, "workload", "") == "learned_256" else LEARNED
     torch.cuda.set_device(0)
     vol = synth.blob_volume(L["shape"], n_blobs=L["n_blobs"], seed=L["seed"], dtype=L["dtype"], noise=0.0,
                             zero_fraction=L["zero_fraction"], device="cuda:0", sigma_scale=L["sigma_scale"])
@@ -449,15 +452,17 @@ def run_learned(args, quiet=False):
     fps = {m: L["tfs"] / (tot[m] / 1000.0) for m in methods}
     held = slice(L["train_tfs"], None)
     fps_held = {m: len(ms[m][held]) / (sum(ms[m][held]) / 1000.0) for m in methods}
-    lat_per_frame = lattice / 10
+    ncensus = min(10, L["tfs"])
+    lat_per_frame = lattice / ncensus
     ls = v.learned_stats()
     line = {
         "metric": METRIC, "value": fps["learned"], "unit": "frames/s", "n_gpus": 1,
         "steps": L["tfs"] * L["frames"], "warmup": L["tfs"], "ms_per_step": tot["learned"] / L["tfs"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
         "data": "synthetic (seeded blobs, 70% zero macrocells, random 16-knot TFs)",
-        "config": {"workload": "learned_1024",
-                   "volume": "1024x1024x1024 u16 (2 GiB), one brick, 256 blobs, 70% zero macrocells",
+        "config": {"workload": "learned_256" if L is LEARNED_SMALL else "learned_1024",
+                   "volume": "x".join(map(str, L["shape"])) + f" u16, one brick, {L['n_blobs']} blobs, "
+                             "70% zero macrocells",
                    "image": f"{w}x{h}", "tfs": L["tfs"], "train_tfs": L["train_tfs"], "step_voxels": L["step"],
                    "early_termination_alpha": L["term"], "judge": f"1 in {L['judge_stride']} tiles, tol 1/255",
                    "l2": "inputs larger than L2 (2 GiB volume resident)"},
@@ -468,7 +473,7 @@ def run_learned(args, quiet=False):
         "speedup": {"learned_vs_plain": fps["learned"] / fps["plain"], "learned_vs_grid": fps["learned"] / fps["grid"],
                     "grid_vs_plain": fps["grid"] / fps["plain"]},
         "gsamples_per_s": {m: lat_per_frame * fps[m] / 1e9 for m in methods},
-        "executed_per_frame": {m: executed[m] / 10 for m in methods}, "lattice_per_frame": lat_per_frame,
+        "executed_per_frame": {m: executed[m] / ncensus for m in methods}, "lattice_per_frame": lat_per_frame,
         "max_abs_diff_8bit_vs_plain": worst,
         "first_frame_ms_median": {m: float(np.median(first_ms[m])) for m in methods},
         "frame_ms_median": {m: float(np.median(ms[m])) for m in methods},
@@ -511,7 +516,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sorted_brick_512",
-                    choices=sorted(WORKLOADS) + ["batch_64x4", "serve_32", "learned_1024"])
+                    choices=sorted(WORKLOADS) + ["batch_64x4", "serve_32", "learned_1024", "learned_256"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--serve-slots", type=int, default=0)
@@ -527,7 +532,7 @@ def main():
         return run_batch(args)
     if args.workload == "serve_32":
         return run_serve(args)
-    if args.workload == "learned_1024":
+    if args.workload in ("learned_1024", "learned_256"):
         return run_learned(args)
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
