@@ -227,7 +227,7 @@ def run_reference(args, wl):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * el / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded blobs; the reference's datasets are not available)",
-            "config": config_of(args, wl),
+            "config": {k: v for k, v in config_of(args, wl).items() if k != "layout"},
             "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
                              "sample": f"each step renders 1/16 of the rows ({band} of {h}); value = steps/16 "
                                        f"frames over the time"},
@@ -497,6 +497,24 @@ def run_learned(args, quiet=False):
     return line
 
 
+def max_over_ranks(values, device):
+    """Each value's maximum over the ranks of the process group (the values
+    themselves without one): the job's time is its slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(x) for x in values]
+    t = torch.tensor([float(x) for x in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def whole_job_rate(steps_per_rank, world, t_ms):
+    """Frames of all ranks per second of the slowest rank (weak scaling:
+    every rank renders its own views)."""
+    return steps_per_rank * world / (t_ms / 1000.0)
+
+
 def _extra(fn, args, keys):
     """A workload's line reduced to `keys`, or the error it raised."""
     import torch
@@ -630,13 +648,10 @@ def main():
             view.render_host(v, tf, states[args.warmup + k], params, host8, sp)
         e2e_s = time.perf_counter() - t0
 
-    t_max = torch.tensor([t_ms, e2e_s * 1000.0], device="cuda")
-    if world > 1:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    t_ms, e2e_ms = float(t_max[0]), float(t_max[1])
+    t_ms, e2e_ms = max_over_ranks([t_ms, e2e_s * 1000.0], "cuda")
+    fps = whole_job_rate(args.steps, world, t_ms)
+    e2e_fps = whole_job_rate(args.steps, world, e2e_ms)
     frames = args.steps * world
-    fps = frames / (t_ms / 1000.0)
-    e2e_fps = frames / (e2e_ms / 1000.0)
     gsps = lattice * world / (t_ms / 1000.0) / 1e9
 
     if rank == 0:
