@@ -538,6 +538,53 @@ int ivr_volume_load(ivr_ctx *c, const void *host, int w, int h, int d, int dtype
     return IVR_OK;
 }
 
+// Streams a raw file to the device: the file is read in chunks into two
+// page-locked staging buffers in turn, each chunk's upload overlapping the
+// next chunk's read; the byte swap runs on the device afterwards.
+static int stream_file(ivr_ctx *c, FILE *fp, const char *path, void *dst, size_t bytes)
+{
+    const size_t chunk = std::min(bytes, (size_t) 64 << 20);
+    void *stage[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaStream_t st = nullptr;
+    bool used[2] = {false, false};
+    int rc = IVR_OK;
+    for (int k = 0; k < 2 && rc == IVR_OK; k++)
+        if (cudaHostAlloc(&stage[k], chunk, cudaHostAllocDefault) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming) != cudaSuccess)
+            rc = fail(c, IVR_ERR_NOMEM, "page-locked staging of %zu bytes", chunk);
+    if (rc == IVR_OK && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+        rc = fail(c, IVR_ERR_CUDA, "upload stream");
+    size_t off = 0;
+    for (int k = 0; rc == IVR_OK && off < bytes; k ^= 1) {
+        const size_t n = std::min(chunk, bytes - off);
+        if (used[k] && cudaEventSynchronize(ev[k]) != cudaSuccess) {
+            rc = fail(c, IVR_ERR_CUDA, "upload of %s", path);
+            break;
+        }
+        const size_t got = fread(stage[k], 1, n, fp);
+        if (got != n) {
+            rc = fail(c, IVR_ERR_IO, "%s: read %zu of %zu bytes", path, off + got, bytes);
+            break;
+        }
+        if (cudaMemcpyAsync((char *) dst + off, stage[k], n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaEventRecord(ev[k], st) != cudaSuccess) {
+            rc = fail(c, IVR_ERR_CUDA, "upload of %s", path);
+            break;
+        }
+        used[k] = true;
+        off += n;
+    }
+    if (st && cudaStreamSynchronize(st) != cudaSuccess && rc == IVR_OK) rc = fail(c, IVR_ERR_CUDA, "upload of %s", path);
+    if (st) cudaStreamDestroy(st);
+    for (int k = 0; k < 2; k++) {
+        if (ev[k]) cudaEventDestroy(ev[k]);
+        if (stage[k]) cudaFreeHost(stage[k]);
+    }
+    cudaGetLastError();
+    return rc;
+}
+
 int ivr_volume_load_file(ivr_ctx *c, const char *path, int w, int h, int d, int dtype, int file_little_endian,
                          ivr_volume **out)
 {
@@ -546,16 +593,34 @@ int ivr_volume_load_file(ivr_ctx *c, const char *path, int w, int h, int d, int 
     if (!path) return fail(c, IVR_ERR_INVALID, "null path");
     if (w < 2 || h < 2 || d < 2 || (dtype != IVR_U8 && dtype != IVR_U16 && dtype != IVR_F32))
         return fail(c, IVR_ERR_INVALID, "bad volume shape or dtype");
-    size_t bytes = (size_t) w * h * d * dtype_size(dtype);
+    if ((long long) w * h * d >= (1LL << 32)) return fail(c, IVR_ERR_UNSUPPORTED, "volume of 2^32 or more voxels");
+    const size_t bytes = (size_t) w * h * d * dtype_size(dtype);
     FILE *fp = fopen(path, "rb");
     if (!fp) return fail(c, IVR_ERR_IO, "cannot open %s", path);
-    std::vector<unsigned char> buf(bytes);
-    size_t got = fread(buf.data(), 1, bytes, fp);
+    setvbuf(fp, nullptr, _IONBF, 0);  // chunks go straight into the staging buffers
+    CK(c, cudaSetDevice(c->device));
+    ivr_volume *v = new ivr_volume();
+    v->ctx = c;
+    v->w = w; v->h = h; v->d = d; v->dtype = dtype;
+    v->full_bytes = bytes;
+    int rc = dev_alloc(c, bytes, &v->d_full);
+    if (rc == IVR_OK) rc = stream_file(c, fp, path, v->d_full, bytes);
     fclose(fp);
-    if (got != bytes) return fail(c, IVR_ERR_IO, "%s: read %zu of %zu bytes", path, got, bytes);
     const uint16_t probe = 1;
-    const int host_little = *(const unsigned char *) &probe == 1;
-    return ivr_volume_load(c, buf.data(), w, h, d, dtype, (file_little_endian ? 1 : 0) != host_little, out);
+    const bool host_little = *(const unsigned char *) &probe == 1;
+    if (rc == IVR_OK && (file_little_endian != 0) != host_little) {
+        const cudaError_t e = launch_byteswap(v->d_full, (long long) w * h * d, (int) dtype_size(dtype), 0);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "byte swap");
+    }
+    if (rc == IVR_OK) rc = setup_bricks(v, 1, 1, 1, 0);
+    if (rc) {
+        const std::string err = c->err;
+        ivr_volume_free(v);
+        c->err = err;
+        return rc;
+    }
+    *out = v;
+    return IVR_OK;
 }
 
 int ivr_volume_free(ivr_volume *v)

@@ -122,6 +122,40 @@ def test_volume_file_bigendian(ctx):
         os.unlink(path)
 
 
+@pytest.mark.parametrize("dtype,little", [("u8", True), ("u16", False), ("f32", True), ("f32", False)])
+def test_volume_file_streams_in_chunks(ctx, dtype, little):
+    """A file larger than one 64 MiB staging chunk: the streamed volume
+    equals the same volume loaded from memory (histogram, min/max and a
+    CONFIG frame)."""
+    shape = {"u8": (260, 512, 512), "u16": (130, 512, 512), "f32": (104, 512, 512)}[dtype]
+    npdt = {"u8": np.uint8, "u16": np.uint16, "f32": np.float32}[dtype]
+    rng = np.random.default_rng(4)
+    vol = (rng.random(shape, dtype=np.float32) * (255.0 if dtype != "u16" else 65535.0)).astype(npdt)
+    assert vol.nbytes > (64 << 20)
+    fd, path = tempfile.mkstemp(suffix=".raw")
+    os.close(fd)
+    try:
+        vol.astype(vol.dtype.newbyteorder("<" if little else ">")).tofile(path)
+        code = {"u8": api.U8, "u16": api.U16, "f32": api.F32}[dtype]
+        a = ctx.load_volume_file(path, shape[2], shape[1], shape[0], code, file_little_endian=little)
+        b = ctx.load_volume(vol)
+        assert a.minmax() == b.minmax()
+        scale = 256.0 / 65536.0 if dtype == "u16" else 1.0
+        tf = ctx.transfer_function().set_lut(synth.ramp_tf(256), 0, scale, api.TF_F2B)
+        frames = []
+        for v in (a, b):
+            view = ctx.view().set(v, orbit_state(35, 25, 64, 48), api.config_params())
+            o32, _ = dev_frame(48, 64)
+            view.render(tf, o32.data_ptr())
+            frames.append(host(o32))
+            view.free()
+        assert np.array_equal(bits(frames[0]), bits(frames[1]))
+        a.free()
+        b.free()
+    finally:
+        os.unlink(path)
+
+
 def test_composite_kernel_matches_reference(ctx):
     import torch
     c = load_case([p for p in GOLDEN if "8bricks" in p][0])
