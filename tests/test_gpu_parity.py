@@ -122,6 +122,28 @@ def test_volume_file_bigendian(ctx):
         os.unlink(path)
 
 
+def test_u16_full_range_colormap_lut(ctx, oracle_mod):
+    """initvolluts on a u16 volume spanning 0..65535: a 65536-entry LUT equal
+    to the oracle's, and the REF frame bitwise equal to O2's."""
+    rng = np.random.default_rng(8)
+    vol = synth.blob_volume((40, 36, 44), n_blobs=8, seed=21, dtype="u16")
+    vol.flat[0], vol.flat[-1] = 0, 65535
+    vol[rng.random(vol.shape) < 0.01] = 65535
+    v = ctx.load_volume(vol)
+    tf = ctx.transfer_function().set_colormap(v, api.CM_SEISMIC, api.TF_SEISMIC2)
+    lut, off = tf.get_lut()
+    ref_lut, ref_off = oracle_mod.lut_for(vol, api.CM_SEISMIC)
+    assert len(lut) == 65536 and off == ref_off == 0
+    assert np.array_equal(lut.view(np.uint32), np.ascontiguousarray(ref_lut, np.float32).view(np.uint32))
+    st = orbit_state(50, 30, 48, 40, fovy=30.0, alpha=1.0)
+    view = ctx.view().set(v, st, api.ref_params())
+    o32, _ = dev_frame(40, 48)
+    view.render(tf, o32.data_ptr())
+    ref = oracle_mod.render(vol, st, ref_lut, ref_off, api.TF_SEISMIC2)
+    assert np.array_equal(bits(host(o32)), bits(ref["rgba32"]))
+    v.free()
+
+
 @pytest.mark.parametrize("dtype,little", [("u8", True), ("u16", False), ("f32", True), ("f32", False)])
 def test_volume_file_streams_in_chunks(ctx, dtype, little):
     """A file larger than one 64 MiB staging chunk: the streamed volume
