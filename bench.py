@@ -516,6 +516,63 @@ def run_learned(args, quiet=False):
     return line
 
 
+def run_ref_preset(args, quiet=True):
+    """The drop-in path with the reference's own semantics (REF preset:
+    ray-parameter step 0.001, 256-sample cap, getlinearsample weights, the
+    SEISMIC2 transfer function over the seismic colormap) on the
+    CPU-runnable configuration (plain_128: 128^3 u8, one brick, 512x512):
+    GPU frames/s, the CPU restatement on the same frames, and a bitwise check
+    of one frame against it."""
+    import torch
+    from oracle import oracle
+    from ivr_gb300 import api
+    wl = WORKLOADS["plain_128"]
+    vol = make_volume(wl, None)
+    w, h = wl["image"]
+    states = views(wl["seed"] + 300, 8, w, h, wl["fovy"])
+    ctx = api.Context(0)
+    v = ctx.load_volume(vol)
+    tf = ctx.transfer_function().set_colormap(v, api.CM_SEISMIC, api.TF_SEISMIC2)
+    view = ctx.view()
+    params = api.ref_params()
+    o32 = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    for st in states[:2]:
+        view.set(v, st, params)
+        view.render(tf, o32.data_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for st in states:
+        view.set(v, st, params)
+        view.render(tf, o32.data_ptr())
+    e1.record()
+    torch.cuda.synchronize()
+    gpu_ms = e0.elapsed_time(e1) / len(states)
+    view.set(v, states[-1], params)
+    view.render(tf, o32.data_ptr())
+    torch.cuda.synchronize()
+    got = o32.cpu().numpy()
+    lut, off = oracle.lut_for(vol, api.CM_SEISMIC)
+    cores = os.cpu_count() or 1
+    prep = oracle.Prepared(vol, (1, 1, 1))
+    t0 = time.perf_counter()
+    n = 0
+    ref = None
+    for st in states[-2:]:
+        ref = oracle.render(vol, st, lut, off, api.TF_SEISMIC2, threads=cores, prepared=prep)
+        n += 1
+    cpu_s = (time.perf_counter() - t0) / n
+    bitwise = bool(np.array_equal(got.view(np.uint32), ref["rgba32"].view(np.uint32)))
+    view.free()
+    tf.free()
+    v.free()
+    ctx.close()
+    return {"workload": "plain_128 (128^3 u8, 512x512), REF preset, SEISMIC2 over the seismic colormap",
+            "fps": 1000.0 / gpu_ms, "cpu_fps": 1.0 / cpu_s, "cpu_cores": cores,
+            "cpu": "the CPU restatement (REF preset) on the same frames, all host threads",
+            "bitwise_equal_to_cpu": bitwise}
+
+
 def max_over_ranks(values, device):
     """Each value's maximum over the ranks of the process group (the values
     themselves without one): the job's time is its slowest rank's."""
@@ -720,6 +777,8 @@ def main():
                                                           "first_frame_ms_median", "config", "clocks"])
         line["serving"] = _extra(run_serve, args, ["value", "unit", "latency_ms", "requests", "rejected",
                                                    "megapixels_per_s", "config", "clocks"])
+        line["ref_preset"] = _extra(run_ref_preset, args, ["workload", "fps", "cpu_fps", "cpu_cores", "cpu",
+                                                           "bitwise_equal_to_cpu"])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -138,9 +138,14 @@ __device__ __forceinline__ float lerpf(float a, float b, float t) { return fmaf(
 
 // CONFIG sampler: trilinear with voxel values at cell corners (the
 // reference's index convention; the halo sits on the high side), clamp to
-// edge.
-template <int DT>
-__device__ __forceinline__ float sample_cfg(const DevBrick &b, float x, float y, float z)
+// edge.  Split in two so that the march's macrocell check can use the cell
+// coordinates of the sample it is about to take.
+struct CellPos {
+    int j, i, k;         // voxel cell, clamped to [0, n-2]
+    float fx, fy, fz;    // position in it, [0, 1]
+};
+
+__device__ __forceinline__ CellPos cell_cfg(const DevBrick &b, float x, float y, float z)
 {
     const int nx = b.nx, ny = b.ny, nz = b.nz;
     float ux = (x - b.bminx) * b.icx;
@@ -152,10 +157,22 @@ __device__ __forceinline__ float sample_cfg(const DevBrick &b, float x, float y,
     ux = fminf(fmaxf(ux, 0.0f), (float) (nx - 1));
     uy = fminf(fmaxf(uy, 0.0f), (float) (ny - 1));
     uz = fminf(fmaxf(uz, 0.0f), (float) (nz - 1));
-    const int j = min(__float2int_rd(ux), nx - 2);
-    const int i = min(__float2int_rd(uy), ny - 2);
-    const int k = min(__float2int_rd(uz), nz - 2);
-    const float fx = ux - (float) j, fy = uy - (float) i, fz = uz - (float) k;
+    CellPos c;
+    c.j = min(__float2int_rd(ux), nx - 2);
+    c.i = min(__float2int_rd(uy), ny - 2);
+    c.k = min(__float2int_rd(uz), nz - 2);
+    c.fx = ux - (float) c.j;
+    c.fy = uy - (float) c.i;
+    c.fz = uz - (float) c.k;
+    return c;
+}
+
+template <int DT>
+__device__ __forceinline__ float fetch_cfg(const DevBrick &b, const CellPos &c)
+{
+    const int nx = b.nx, ny = b.ny;
+    const int j = c.j, i = c.i, k = c.k;
+    const float fx = c.fx, fy = c.fy, fz = c.fz;
     float c00, c10, c01, c11;
     if (b.quad) {
         // corner-packed copy: the cell's 8 voxels in two vector loads
@@ -184,6 +201,12 @@ __device__ __forceinline__ float sample_cfg(const DevBrick &b, float x, float y,
     float c0 = lerpf(c00, c10, fy);
     float c1 = lerpf(c01, c11, fy);
     return lerpf(c0, c1, fz);
+}
+
+template <int DT>
+__device__ __forceinline__ float sample_cfg(const DevBrick &b, float x, float y, float z)
+{
+    return fetch_cfg<DT>(b, cell_cfg(b, x, y, z));
 }
 
 __device__ __forceinline__ float4 lut_at(const FrameDesc &f, int idx)
@@ -352,10 +375,11 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
     for (int i = i0; i < i1; i++) {
         const float t = cfg_t(t0, dt, i);
         const float x = fmaf(dx, t, ox), y = fmaf(dy, t, oy), z = fmaf(dz, t, oz);
+        const CellPos c0 = cell_cfg(b, x, y, z);
         if (SKIP && i >= icheck) {
-            const int cj = min(max(__float2int_rd((x - b.bminx) * b.icx), 0), b.nx - 2) / kCell;
-            const int ci = min(max(__float2int_rd((y - b.bminy) * b.icy), 0), b.ny - 2) / kCell;
-            const int ck = min(max(__float2int_rd((z - b.bminz) * b.icz), 0), b.nz - 2) / kCell;
+            // the sample's macrocell: its voxel cell (the sampler's own index
+            // arithmetic) over 16
+            const int cj = c0.j / kCell, ci = c0.i / kCell, ck = c0.k / kCell;
             // r >= 1: the cube of cells within r-1 of this one is transparent
             const int r = empty[((long long) ck * b.mcy + ci) * b.mcx + cj];
             const int rr = max(r, 1);
@@ -382,7 +406,7 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
         if (PAIR && !CENSUS) {
             const int lim = SKIP ? min(i1, icheck) : i1;
             const float t1 = cfg_t(t0, dt, i + 1);
-            const float s0 = sample_cfg<DT>(b, x, y, z);
+            const float s0 = fetch_cfg<DT>(b, c0);
             const float s1 = sample_cfg<DT>(b, fmaf(dx, t1, ox), fmaf(dy, t1, oy), fmaf(dz, t1, oz));
             const float4 e0 = lut_at(f, (int) (s0 * f.lut_scale) - f.lut_off);
             const float4 e1 = lut_at(f, (int) (s1 * f.lut_scale) - f.lut_off);
@@ -409,7 +433,7 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
             }
             continue;
         }
-        const float s = sample_cfg<DT>(b, x, y, z);
+        const float s = fetch_cfg<DT>(b, c0);
         if (CENSUS) {
             nexec++;
             int j = min(max((int) floorf((x - b.bminx) * b.icx), 0), b.nx - 2) / kCell;
