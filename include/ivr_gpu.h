@@ -153,6 +153,14 @@ int ivr_volume_free(ivr_volume *vol);
  * (getlocalbrick).  Each brick becomes its own device array.  The default
  * after load is one brick. */
 int ivr_bricks_setup(ivr_volume *vol, int py, int px, int pz, int overlap);
+/* Per-voxel gradient, as gradient3d (mathutil.c:242-325, built under
+ * -DGRAD at main.c:1181-1196) intends it: grad4_dev receives w*h*d float4
+ * (gx, gy, gz, |g|) in the volume's [d][h][w] order; per axis a central
+ * difference halved inside and (V(1)-V(0))/2, (V(n-1)-V(n-2))/2 on the
+ * faces.  The reference's own code writes every voxel to offset i*j*k,
+ * takes its last z face from the two slabs before it and leaves edges and
+ * corners unwritten; those are fixed here.  Queued on `stream`. */
+int ivr_volume_gradient(ivr_volume *vol, float *grad4_dev, void *stream);
 /* Corner-packed brick copies (no counterpart in the reference; on by
  * default).  Each brick gets a second copy in which element (j, i, k) holds
  * the four voxels (j, i), (j+1, i), (j, i+1), (j+1, i+1) of slab k, so a

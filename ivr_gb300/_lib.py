@@ -114,6 +114,7 @@ SIGNATURES = {
     "ivr_volume_free": (_I, [_P]),
     "ivr_bricks_setup": (_I, [_P, _I, _I, _I, _I]),
     "ivr_volume_set_quads": (_I, [_P, _I]),
+    "ivr_volume_gradient": (_I, [_P, _P, _P]),
     "ivr_volume_quad_bytes": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
     "ivr_volume_minmax": (_I, [_P, _PF, _PF]),
     "ivr_volume_histogram": (_I, [_P, _PI, _I]),

@@ -159,6 +159,10 @@ class Volume:
         self.ctx.check(self.ctx.lib.ivr_bricks_setup(self.h, py, px, pz, overlap))
         return self
 
+    def gradient(self, out_dev, stream=None):
+        """Per-voxel (gx, gy, gz, |g|) into out_dev: float32 [d][h][w][4]."""
+        self.ctx.check(self.ctx.lib.ivr_volume_gradient(self.h, _vp(out_dev), _vp(stream)))
+
     def quads(self, on: bool) -> "Volume":
         """Corner-packed brick copies on/off (on by default)."""
         self.ctx.check(self.ctx.lib.ivr_volume_set_quads(self.h, int(on)))

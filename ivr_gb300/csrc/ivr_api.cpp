@@ -639,6 +639,15 @@ int ivr_bricks_setup(ivr_volume *v, int py, int px, int pz, int overlap)
     return setup_bricks(v, py, px, pz, overlap);
 }
 
+int ivr_volume_gradient(ivr_volume *v, float *grad4_dev, void *stream)
+{
+    if (!v) return IVR_ERR_INVALID;
+    if (!grad4_dev) return fail(v->ctx, IVR_ERR_INVALID, "null gradient output");
+    CK(v->ctx, cudaSetDevice(v->ctx->device));
+    CK(v->ctx, launch_gradient(v->d_full, v->dtype, v->w, v->h, v->d, (float4 *) grad4_dev, (cudaStream_t) stream));
+    return IVR_OK;
+}
+
 int ivr_volume_set_quads(ivr_volume *v, int on)
 {
     if (!v) return IVR_ERR_INVALID;

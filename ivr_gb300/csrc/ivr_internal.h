@@ -139,6 +139,8 @@ cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int n
                               int mcz, cudaStream_t s);
 cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const int *nzprefix, int lut_n,
                                int lut_off, float lut_scale, uint8_t *empty, cudaStream_t s);
+// per-voxel gradient (gx, gy, gz, |g|) of a w x h x d volume into out
+cudaError_t launch_gradient(const void *data, int dtype, int w, int h, int d, float4 *out, cudaStream_t s);
 // corner-packed copy of an nx x ny x nz brick: (nx-1)(ny-1)nz four-voxel
 // elements of 4 * sizeof(dtype) bytes
 size_t quad_bytes(int dtype, int nx, int ny, int nz);

@@ -382,6 +382,46 @@ cudaError_t launch_dist_relax(uint8_t *dist, int mcx, int mcy, int mcz, cudaStre
     return cudaGetLastError();
 }
 
+// Per-voxel gradient (gradient3d, restated as intended): per axis a halved
+// central difference inside and a halved one-sided difference on the
+// faces, times the unit spacing; w = |(x, y, z)| as mag3f computes it.
+template <typename T>
+__device__ __forceinline__ float grad_axis(const T *v, long long o, int c, int n, long long stride)
+{
+    if (c == 0) return ((float) v[o + stride] - (float) v[o]) / 2.0f * 1.0f;
+    if (c == n - 1) return ((float) v[o] - (float) v[o - stride]) / 2.0f * 1.0f;
+    return ((float) v[o + stride] - (float) v[o - stride]) / 2.0f * 1.0f;
+}
+
+template <typename T>
+__global__ void gradient_kernel(const T *vol, int w, int h, int d, float4 *out)
+{
+    const long long n = (long long) w * h * d;
+    for (long long o = blockIdx.x * (long long) blockDim.x + threadIdx.x; o < n;
+         o += (long long) gridDim.x * blockDim.x) {
+        const int j = (int) (o % w);
+        const long long r = o / w;
+        const int i = (int) (r % h), k = (int) (r / h);
+        const float x = grad_axis(vol, o, j, w, 1);
+        const float y = grad_axis(vol, o, i, h, w);
+        const float z = grad_axis(vol, o, k, d, (long long) w * h);
+        out[o] = make_float4(x, y, z, sqrtf(x * x + y * y + z * z));
+    }
+}
+
+cudaError_t launch_gradient(const void *data, int dtype, int w, int h, int d, float4 *out, cudaStream_t s)
+{
+    const long long n = (long long) w * h * d;
+    const int grid = grid_for(n, 256);
+    switch (dtype) {
+    case IVR_U8: gradient_kernel<<<grid, 256, 0, s>>>((const uint8_t *) data, w, h, d, out); break;
+    case IVR_U16: gradient_kernel<<<grid, 256, 0, s>>>((const uint16_t *) data, w, h, d, out); break;
+    case IVR_F32: gradient_kernel<<<grid, 256, 0, s>>>((const float *) data, w, h, d, out); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
 template <typename T, typename V>
 __global__ void quad_kernel(const T *src, int nx, int ny, int nz, V *dst)
 {

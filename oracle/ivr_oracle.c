@@ -981,3 +981,35 @@ void orc_macrocells(const float *vol, int w, int h, int d, int cell, float *cmin
                 cmax[c] = hi;
             }
 }
+
+/* gradient3d (mathutil.c:242-325) with grad() (mathutil.c:326-337) and the
+ * index map maptoffset3d (mathutil.h:139-143): per voxel (row i, column j,
+ * slab k) x from columns, y from rows, z from slabs; a central difference
+ * halved inside, (V(1) - V(0)) / 2 and (V(n-1) - V(n-2)) / 2 on the faces
+ * (the reference's face formulas), then times the unit spacing, and
+ * w = mag3f(x, y, z) (mathutil.c:233-236).  Restated as intended: the
+ * reference writes every voxel to offset i*j*k, takes the k = p-1 face from
+ * k-1 and k-2, and leaves edges and corners unwritten; here every voxel gets
+ * the per-axis rule at its own offset. */
+static float grad_axis(const float *v, long long o, int c, int n, long long stride)
+{
+    if (c == 0) return (v[o + stride] - v[o]) / 2.0f * 1.0f;
+    if (c == n - 1) return (v[o] - v[o - stride]) / 2.0f * 1.0f;
+    return (v[o + stride] - v[o - stride]) / 2.0f * 1.0f;
+}
+
+void orc_gradient(const float *vol, int w, int h, int d, float *out)
+{
+    for (int k = 0; k < d; k++)
+        for (int i = 0; i < h; i++)
+            for (int j = 0; j < w; j++) {
+                const long long o = ((long long) k * h + i) * w + j;
+                const float x = grad_axis(vol, o, j, w, 1);
+                const float y = grad_axis(vol, o, i, h, w);
+                const float z = grad_axis(vol, o, k, d, (long long) w * h);
+                out[4 * o + 0] = x;
+                out[4 * o + 1] = y;
+                out[4 * o + 2] = z;
+                out[4 * o + 3] = sqrtf(x * x + y * y + z * z);
+            }
+}

@@ -103,6 +103,8 @@ void orc_histogram(const void *data, int dtype, long long n, float mn, int hsize
 
 /* Macrocell min/max over cells of `cell` voxels plus the +1 boundary layer
  * (what a trilinear sample in the cell can read). */
+/* per-voxel gradient (gx, gy, gz, |g|) of a [d][h][w] float volume */
+void orc_gradient(const float *vol, int w, int h, int d, float *out);
 void orc_macrocells(const float *vol, int w, int h, int d, int cell,
                     float *cmin, float *cmax);
 

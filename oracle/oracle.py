@@ -96,6 +96,7 @@ def o2():
         lib.orc_histogram.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_float,
                                       ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
         lib.orc_macrocells.argtypes = [_FP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _FP, _FP]
+        lib.orc_gradient.argtypes = [_FP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _FP]
         _o2 = lib
     return _o2
 
@@ -249,6 +250,15 @@ def macrocells(vol: np.ndarray, cell=16):
     mx = np.zeros(shp, np.float32)
     o2().orc_macrocells(_fp(v), w, h, d, cell, _fp(mn), _fp(mx))
     return mn, mx
+
+
+def gradient(vol: np.ndarray) -> np.ndarray:
+    """Per-voxel (gx, gy, gz, |g|) of the volume as float32 [d][h][w][4]."""
+    v = np.ascontiguousarray(vol, np.float32)
+    d, h, w = v.shape
+    out = np.zeros((d, h, w, 4), np.float32)
+    o2().orc_gradient(_fp(v), w, h, d, _fp(out))
+    return out
 
 
 def ref_render(vol: np.ndarray, state: IvrState, colormap_id: int, xfer: int, procdims=(1, 1, 1), tile=(1, 1),

@@ -122,6 +122,21 @@ def test_volume_file_bigendian(ctx):
         os.unlink(path)
 
 
+@pytest.mark.parametrize("dtype", ["u8", "u16", "f32"])
+def test_gradient_matches_oracle(ctx, oracle_mod, dtype):
+    """ivr_volume_gradient bitwise against the restated gradient3d, every
+    voxel (faces, edges and corners included)."""
+    import torch
+    vol = synth.blob_volume((19, 23, 29), n_blobs=6, seed=17, dtype=dtype, noise=0.05)
+    v = ctx.load_volume(vol)
+    out = torch.full((19, 23, 29, 4), -1.0, dtype=torch.float32, device="cuda")
+    v.gradient(out.data_ptr())
+    got = host(out)
+    ref = oracle_mod.gradient(vol.astype(np.float32))
+    assert np.array_equal(bits(got), bits(ref))
+    v.free()
+
+
 def test_u16_full_range_colormap_lut(ctx, oracle_mod):
     """initvolluts on a u16 volume spanning 0..65535: a 65536-entry LUT equal
     to the oracle's, and the REF frame bitwise equal to O2's."""

@@ -149,3 +149,25 @@ def test_config_skip_lossless_in_oracle(oracle_mod, procdims):
     b = oracle_mod.render(vol, st, lut, 0, 6, preset=1, procdims=procdims, skip=True)
     assert np.array_equal(bits(a["rgba32"]), bits(b["rgba32"]))
     assert b["stats"]["samples_exec"] < a["stats"]["samples_exec"]
+
+
+def test_gradient_rule(oracle_mod):
+    """gradient3d as intended: per axis a halved central difference inside
+    and a halved one-sided difference on the faces, on every voxel, edges
+    and corners included; w = |g| summed in x, y, z order."""
+    rng = np.random.default_rng(3)
+    v = rng.random((6, 5, 7)).astype(np.float32) * 100
+    g = oracle_mod.gradient(v)
+
+    def axis(a, ax):
+        a = np.moveaxis(a, ax, -1)
+        out = np.empty_like(a)
+        out[..., 1:-1] = (a[..., 2:] - a[..., :-2]) / np.float32(2)
+        out[..., 0] = (a[..., 1] - a[..., 0]) / np.float32(2)
+        out[..., -1] = (a[..., -1] - a[..., -2]) / np.float32(2)
+        return np.moveaxis(out, -1, ax)
+
+    gx, gy, gz = axis(v, 2), axis(v, 1), axis(v, 0)
+    assert np.array_equal(g[..., 0], gx) and np.array_equal(g[..., 1], gy) and np.array_equal(g[..., 2], gz)
+    mag = np.sqrt((gx * gx + gy * gy) + gz * gz).astype(np.float32)
+    assert np.array_equal(g[..., 3], mag)
