@@ -443,7 +443,7 @@ def run_learned(args, quiet=False):
         for t, (tf, st) in enumerate(zip(tfs, states)):
             for m, skip in methods.items():
                 p = api.config_params(step=L["step"], term_alpha=L["term"], skip=skip,
-                                      judge_stride=L["judge_stride"])
+                                      judge_stride=getattr(args, "judge_stride", 0) or L["judge_stride"])
                 view = vw[m].set(v, st, p)
                 # first frame of a new TF: includes building its grid
                 torch.cuda.synchronize()
@@ -616,6 +616,7 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=0)
     ap.add_argument("--serve-batch", type=int, default=0)
     ap.add_argument("--serve-rate", default="", help="per-client request rate range lo,hi (req/s)")
+    ap.add_argument("--judge-stride", type=int, default=0, help="learned skipping: judge 1 in this many tiles")
     ap.add_argument("--linear", action="store_true",
                     help="render from the bricks themselves, without the corner-packed copies")
     ap.add_argument("--no-extras", action="store_true",
