@@ -266,6 +266,44 @@ def test_config_preset_matches_o2(ctx, oracle_mod, case, quads):
     v.free()
 
 
+CONFIG_EXTRA = [
+    # shape, dtype, procdims, az, el, win, tile, alpha, clip, term
+    ((40, 36, 44), "u8", (1, 1, 1), 20, 15, (70, 50), (8, 8), 1.0, None, 0.99),      # viewport rounded to tiles
+    ((44, 40, 36), "f32", (3, 1, 2), 130, -25, (64, 48), (1, 1), 1.0, None, 0.99),   # 3x1x2 bricks, remainders
+    ((40, 40, 40), "u16", (2, 2, 2), 75, 35, (56, 56), (1, 1), 0.5, None, 0.99),     # opacity scale 0.5
+    ((40, 40, 40), "u8", (2, 1, 1), 200, 5, (48, 48), (1, 1), 0.0, None, 0.99),      # opacity scale 0
+    ((40, 40, 40), "u8", (1, 2, 1), 310, -40, (60, 44), (1, 1), 1.0, None, 2.0),     # no termination
+    ((48, 40, 44), "f32", (2, 2, 2), 45, 25, (64, 64), (1, 1), 1.0,
+     (0.6, 0.8, 0.7, 0.5, 0.9, 0.4), 0.99),                                          # clip planes
+]
+
+
+@pytest.mark.parametrize("quads", [True, False], ids=["quads", "linear"])
+@pytest.mark.parametrize("case", CONFIG_EXTRA, ids=["tiles", "3x1x2", "alpha0.5", "alpha0", "noterm", "clip"])
+def test_config_more_cases_match_o2(ctx, oracle_mod, case, quads):
+    shape, dtype, procdims, az, el, win, tile, alpha, clip, term = case
+    vol = make_config_volume(shape, dtype, 11)
+    lut = synth.ramp_tf(256)
+    scale = 256.0 / 65536.0 if dtype == "u16" else 1.0
+    st = orbit_state(az, el, win[0], win[1], fovy=30.0, alpha=alpha, clip=clip)
+    ref = oracle_mod.render(vol, st, lut, 0, 6, preset=1, procdims=procdims, term_alpha=term, lut_scale=scale,
+                            tile=tile)
+    v = ctx.load_volume(vol).quads(quads)
+    if np.prod(procdims) > 1:
+        v.bricks(*procdims)
+    tf = ctx.transfer_function().set_lut(lut, 0, scale, api.TF_F2B)
+    view = ctx.view().set(v, st, api.config_params(term_alpha=term, tile=tile))
+    vh, vw = ref["rgba32"].shape[:2]
+    assert (view.info()["vw"], view.info()["vh"]) == (vw, vh)
+    o32, o8 = dev_frame(vh, vw)
+    view.render(tf, o32.data_ptr(), o8.data_ptr())
+    assert np.array_equal(bits(host(o32)), bits(ref["rgba32"]))
+    assert np.array_equal(host(o8), ref["rgba8"])
+    if alpha == 0.0:
+        assert not ref["rgba32"].any()
+    v.free()
+
+
 def test_config_skip_is_lossless_and_cheaper(ctx):
     vol = make_config_volume((64, 64, 64), "u8", 3)
     lut = synth.ramp_tf(256)
