@@ -650,14 +650,30 @@ __global__ void __launch_bounds__(kThreads, JUDGE ? kJudgeBlocksPerSm : kCfgBloc
     int worst = 0;
     unsigned judged = 0;
     const bool exact = JUDGE && *(volatile const int *) f.learned_bad != 0;
+    // judged launches hand out the judged tiles (judge_phase modulo
+    // judge_stride) first, so that their second march is spread over the
+    // launch instead of stretching its end; the other tiles follow in order
+    const long long njudged =
+        JUDGE ? (ntiles > f.judge_phase ? (ntiles - f.judge_phase + f.judge_stride - 1) / f.judge_stride : 0) : 0;
     for (;;) {
         unsigned long long ticket = 0;
         if (lane == 0) ticket = atomicAdd(f.tickets, 1ull);
-        const long long tile = (long long) (__shfl_sync(0xffffffffu, ticket, 0) - f.ticket_base);
-        if (tile >= ntiles) break;
+        const long long q = (long long) (__shfl_sync(0xffffffffu, ticket, 0) - f.ticket_base);
+        if (q >= ntiles) break;
+        long long tile = q;
+        if (JUDGE) {
+            if (q < njudged) {
+                tile = q * f.judge_stride + f.judge_phase;
+            } else {
+                // the (q - njudged)-th tile that is not judged
+                const long long r = q - njudged, per = f.judge_stride - 1;
+                const long long o = r % per;
+                tile = (r / per) * f.judge_stride + (o < f.judge_phase ? o : o + 1);
+            }
+        }
         const int oi = (int) (tile / tiles_x) * 4 + (lane >> 3), oj = (int) (tile % tiles_x) * 8 + (lane & 7);
         pixel_cfg<DT, SKIP, CENSUS, kPair>(f, oi, oj, out32, out8, nexec, nlat, exact);
-        if (JUDGE && !exact && tile % f.judge_stride == f.judge_phase) {
+        if (JUDGE && !exact && q < njudged) {
             const int i = f.out_y + oi, j = f.out_x + oj;
             if (oi < f.out_h && oj < f.out_w && i < f.vh && j < f.vw) {
                 const float4 ex = ray_cfg<DT, true, false, kPair>(f, i, j, nexec, nlat, true);
