@@ -88,6 +88,38 @@ __device__ __forceinline__ bool ray_box(const float *dc, float ox, float oy, flo
     return tin < tout && (tin > 0.0f || tout > 0.0f);
 }
 
+// The CONFIG slab test: ray_box's planes and visiting order, with each hit
+// parameter taken as +-numer times the ray's reciprocal direction component
+// (id*) instead of a division -- the CONFIG lattice's own definition; the
+// REF preset keeps the reference's division.  For the axis-aligned normals
+// numer = d -+ o and denom = +-d exactly, so only the rounding of the hit
+// parameters differs from ray_box.
+__device__ __forceinline__ bool ray_box_cfg(const float *dc, float ox, float oy, float oz, float dx, float dy,
+                                            float dz, float idx, float idy, float idz, float &tin, float &tout)
+{
+    tin = -FLT_MAX;
+    tout = FLT_MAX;
+#pragma unroll
+    for (int p = 0; p < 6; p++) {
+        const int axis = p >> 1;
+        const bool pos = (p & 1) != 0;
+        const float o = axis == 0 ? ox : axis == 1 ? oy : oz;
+        const float d = axis == 0 ? dx : axis == 1 ? dy : dz;
+        const float id = axis == 0 ? idx : axis == 1 ? idy : idz;
+        const float numer = pos ? dc[p] - o : dc[p] + o;
+        if (tin < tout) {
+            if (d == 0.0f) {
+                if (numer < 0.0f) tin = tout + 1.0f;
+            } else {
+                const float thit = (pos ? numer : -numer) * id;
+                if (pos ? d > 0.0f : d < 0.0f) tout = fminf(tout, thit);
+                else tin = fmaxf(tin, thit);
+            }
+        }
+    }
+    return tin < tout && (tin > 0.0f || tout > 0.0f);
+}
+
 // getlinearsample (ray.c:87-181, non-BGQ branch), quirks included: the
 // weights are scaled by the cell size squared, and the x weight blends the
 // +1 row (y) neighbour.  x + fabs(min.x) is a double sum in the reference,
@@ -362,7 +394,7 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
                           unsigned long long &nexec, unsigned long long &nlat)
 {
     float tin, tout;
-    if (!ray_box(b.dconst, f.origx, f.origy, f.origz, dx, dy, dz, tin, tout)) return;
+    if (!ray_box_cfg(b.dconst, f.origx, f.origy, f.origz, dx, dy, dz, idx, idy, idz, tin, tout)) return;
     const int i0 = cfg_first_ge(t0, dt, idt, tin);
     const int i1 = cfg_first_ge(t0, dt, idt, tout);
     if (CENSUS) {
@@ -533,13 +565,14 @@ __device__ __forceinline__ float4 ray_cfg(const FrameDesc &f, int i, int j, unsi
     const float dx = f.ctm[0] * u + f.ctm[1] * v + f.ctm[2] * f.eyen;
     const float dy = f.ctm[3] * u + f.ctm[4] * v + f.ctm[5] * f.eyen;
     const float dz = f.ctm[6] * u + f.ctm[7] * v + f.ctm[8] * f.eyen;
+    const float idx = 1.0f / dx, idy = 1.0f / dy, idz = 1.0f / dz;
     float tin, tout;
-    if (!ray_box(f.gdconst, f.origx, f.origy, f.origz, dx, dy, dz, tin, tout)) return acc;
+    if (!ray_box_cfg(f.gdconst, f.origx, f.origy, f.origz, dx, dy, dz, idx, idy, idz, tin, tout)) return acc;
     const float t0 = tin > 0.0f ? tin : 0.0f;
     const float len = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
     const float dt = f.step / len;
     bool done = !(dt > 0.0f);
-    const float idx = 1.0f / dx, idy = 1.0f / dy, idz = 1.0f / dz, idt = 1.0f / dt;
+    const float idt = 1.0f / dt;
     for (int s = 0; s < f.nb && (CENSUS || !done); s++) {
         const int k = f.order[s];
         if (f.single >= 0 && k != f.single) continue;

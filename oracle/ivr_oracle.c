@@ -314,6 +314,35 @@ static int ray_box(const float dconst[6], v3 o, v3 d, float *tin, float *tout)
     return 0;
 }
 
+/* The CONFIG slab test: ray_box's planes and order, each hit parameter
+ * +-numer times the reciprocal direction component (the CONFIG lattice's
+ * definition; REF keeps the reference's division).  With the axis-aligned
+ * normals numer = d -+ o and denom = +-d exactly. */
+static int ray_box_cfg(const float dconst[6], v3 o, v3 d, v3 id, float *tin, float *tout)
+{
+    *tin = -FLT_MAX;
+    *tout = FLT_MAX;
+    for (int p = 0; p < 6 && *tin < *tout; p++) {
+        int axis = p >> 1, pos = p & 1;
+        float oa = axis == 0 ? o.x : axis == 1 ? o.y : o.z;
+        float da = axis == 0 ? d.x : axis == 1 ? d.y : d.z;
+        float ia = axis == 0 ? id.x : axis == 1 ? id.y : id.z;
+        float numer = pos ? dconst[p] - oa : dconst[p] + oa;
+        if (da == 0.0f) {
+            if (numer < 0.0f) *tin = *tout + 1.0f;
+        } else {
+            float thit = (pos ? numer : -numer) * ia;
+            if (pos ? da > 0.0f : da < 0.0f) *tout = fminf(*tout, thit);
+            else *tin = fmaxf(*tin, thit);
+        }
+    }
+    if (*tin < *tout) {
+        if (*tin > 0.0f) return 1;
+        if (*tout > 0.0f) return 1;
+    }
+    return 0;
+}
+
 static int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 /* getlinearsample, non-BGQ branch (ray.c:87-181), quirks included:
@@ -543,7 +572,8 @@ static void march_cfg(const orc_scene *sc, const brick_t *b, v3 o, v3 d, float t
                       const tf_t *tf, acc_t *acc, long long *nalg, long long *nexec)
 {
     float tin, tout;
-    if (!ray_box(b->dconst, o, d, &tin, &tout)) return;
+    v3 id = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+    if (!ray_box_cfg(b->dconst, o, d, id, &tin, &tout)) return;
     int i0 = cfg_first_ge(t0, dt, tin);
     int i1 = cfg_first_ge(t0, dt, tout);
     if (i1 <= i0) return;
@@ -781,8 +811,9 @@ int orc_render_prepared(const orc_scene *sc, const orc_prepared *prep, int nthre
                 for (int k = 0; k < K; k++) any |= in_rect(&bs[k], i, j);
                 if (!any) continue;
                 v3 d = cfg_dir(&v, i, j);
+                v3 id = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
                 float tin, tout;
-                if (!ray_box(gdconst, v.orig, d, &tin, &tout)) continue;
+                if (!ray_box_cfg(gdconst, v.orig, d, id, &tin, &tout)) continue;
                 float t0 = tin > 0.0f ? tin : 0.0f;
                 float len = sqrtf(fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x)));
                 float dt = step_world / len;
