@@ -310,6 +310,7 @@ int frame_for(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single
     f.judge = nullptr;
     f.judge_reject = nullptr;
     f.learned_bad = nullptr;
+    f.judge8 = nullptr;
     if (view->p.skip != IVR_SKIP_NONE && view->p.preset == IVR_PRESET_CONFIG) {
         // a learned grid comes with the exact one (the judge's and the
         // fallback's), unless the judge has rejected it: then only the exact
@@ -382,10 +383,21 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
         f.judge_phase = (int) (view->judge_frame++ % (unsigned long long) view->p.judge_stride);
         f.judge_tol = view->p.judge_tol;
         for (int k = 0; k < f.nb; k++) f.exact[k] = exact->dist[k];
+        const size_t need = (size_t) std::max(judge_scratch_bytes(f), (long long) sizeof(uchar4));
+        if (view->judge_bytes < need) {
+            dev_free(c, view->d_judge8, view->judge_bytes);
+            view->d_judge8 = nullptr;
+            view->judge_bytes = 0;
+            rc = dev_alloc(c, need, (void **) &view->d_judge8);
+            if (rc) return rc;
+            view->judge_bytes = need;
+        }
+        f.judge8 = view->d_judge8;
     }
     rc = launch_view(view, f, o32, o8, s);
     if (rc) return rc;
     if (judged) {
+        CK(c, launch_judge_compare(f, (const uchar4 *) o8, (const float4 *) o32, s));
         FrameDesc ff = f;
         ff.judge = nullptr;
         for (int k = 0; k < ff.nb; k++) ff.b[k].empty = exact->dist[k];
@@ -827,6 +839,7 @@ int ivr_view_free(ivr_view *v)
     if (!v) return IVR_ERR_INVALID;
     dev_free(v->ctx, v->d_tickets, sizeof(unsigned long long));
     dev_free(v->ctx, v->d_judge, sizeof(JudgeWords));
+    dev_free(v->ctx, v->d_judge8, v->judge_bytes);
     delete v;
     return IVR_OK;
 }

@@ -86,8 +86,11 @@ struct ivr_view {
     bool valid = false;
     ivr::FrameDesc f{};
     ivr_frame_info info{};
-    // learned-skip judge: the per-frame verdict words and running totals
+    // learned-skip judge: the per-frame verdict words and running totals,
+    // and the scratch of the judged tiles' exact re-march
     int *d_judge = nullptr;                 // ivr::JudgeWords
+    uchar4 *d_judge8 = nullptr;
+    size_t judge_bytes = 0;
     unsigned long long judge_frame = 0;     // rotates the sampled tiles
 };
 

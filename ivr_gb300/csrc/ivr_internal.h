@@ -86,6 +86,7 @@ struct FrameDesc {
     int *learned_bad;                // nonzero: the learned grid is wrong,
                                      // render with the exact grids
     int judge_stride, judge_phase, judge_tol;
+    uchar4 *judge8;                  // the judged tiles' exact re-march, 32 pixels each
     int order[kMaxBricks];   // near -> far
     DevBrick b[kMaxBricks];
     const uint8_t *exact[kMaxBricks];  // the exact grids (judged launches)
@@ -164,6 +165,10 @@ cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaSt
 // thread (sample_peak_threads())
 cudaError_t launch_sample_peak(const FrameDesc &f, int steps, float4 *out, long long *samples, cudaStream_t s);
 int sample_peak_threads();
+// the verdict of a learned-skip frame rendered by a judged launch of f
+cudaError_t launch_judge_compare(const FrameDesc &f, const uchar4 *out8, const float4 *out32, cudaStream_t s);
+// bytes of f.judge8 a judged launch of f writes
+long long judge_scratch_bytes(const FrameDesc &f);
 // transparent-radius relaxation of a flag grid (kDistCap or 0 per cell)
 cudaError_t launch_dist_relax(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s);
 // batched CONFIG frames of one volume dtype; *ticket must be zero at launch

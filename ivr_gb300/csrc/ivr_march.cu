@@ -604,34 +604,28 @@ __device__ __forceinline__ float4 pixel_cfg(const FrameDesc &f, int oi, int oj, 
     return acc;
 }
 
-// Largest channel difference between a pixel this thread stored (out8, or
-// out32 quantised) and the exact march's colour.
-__device__ __forceinline__ int q8_diff(const uchar4 *out8, const float4 *out32, long long o, float4 b)
-{
-    uchar4 a;
-    if (out8) {
-        a = out8[o];
-    } else {
-        const float4 v = out32[o];
-        a = make_uchar4(q8(v.x), q8(v.y), q8(v.z), q8(v.w));
-    }
-    const int dx = abs((int) a.x - (int) q8(b.x)), dy = abs((int) a.y - (int) q8(b.y));
-    const int dz = abs((int) a.z - (int) q8(b.z)), dw = abs((int) a.w - (int) q8(b.w));
-    return max(max(dx, dy), max(dz, dw));
-}
+// What the judge's verdict needs (from the frame descriptor).
+struct JudgeArgs {
+    JudgeWords *judge;
+    int *judge_reject;
+    int *learned_bad;
+    int judge_tol;
+};
 
-// End of a judged launch for one warp: its largest difference and pixel
+// End of a judge launch for one warp: its largest difference and pixel
 // count go into the judge words; the launch's last warp sets the verdict
 // (fail = largest difference > tolerance), adds it to the totals, marks the
-// learned grid rejected on failure and clears the per-frame words.
-__device__ __forceinline__ void judge_finish(const FrameDesc &f, int worst, unsigned judged, bool exact)
+// learned grid wrong on failure and clears the per-frame words.  A grid
+// already marked wrong was not used (the frame marched with the exact
+// grid): nothing is judged and the frame counts as an exact one.
+__device__ __forceinline__ void judge_finish(const JudgeArgs &a, int worst, unsigned judged, bool known_bad)
 {
     for (int o = 16; o > 0; o >>= 1) {
         worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
         judged += __shfl_xor_sync(0xffffffffu, judged, o);
     }
     if ((threadIdx.x & 31) != 0) return;
-    JudgeWords *jw = f.judge;
+    JudgeWords *jw = a.judge;
     if (worst > 0) atomicMax(&jw->maxdiff, worst);
     if (judged) atomicAdd(&jw->pixels, (unsigned long long) judged);
     __threadfence();
@@ -639,9 +633,9 @@ __device__ __forceinline__ void judge_finish(const FrameDesc &f, int worst, unsi
     if (atomicAdd(&jw->warps_done, 1) != warps - 1) return;
     __threadfence();
     const int m = atomicAdd(&jw->maxdiff, 0);
-    const int failed = m > f.judge_tol;
+    const int failed = m > a.judge_tol;
     jw->fail = failed;
-    if (exact) {
+    if (known_bad) {
         jw->exact_frames += 1;
     } else {
         jw->frames += 1;
@@ -649,12 +643,18 @@ __device__ __forceinline__ void judge_finish(const FrameDesc &f, int worst, unsi
         if (m > jw->worst) jw->worst = m;
     }
     if (failed) {
-        *f.learned_bad = 1;
-        *(volatile int *) f.judge_reject = 1;
+        *a.learned_bad = 1;
+        *(volatile int *) a.judge_reject = 1;
         __threadfence_system();
     }
     jw->maxdiff = 0;
     jw->warps_done = 0;
+}
+
+// Tiles judged in a frame: judge_phase, judge_phase + judge_stride, ...
+__host__ __device__ inline long long judged_tiles(long long ntiles, int stride, int phase)
+{
+    return ntiles > phase ? (ntiles - phase + stride - 1) / stride : 0;
 }
 
 // CONFIG kernel, persistent: every warp takes 8x4 pixel tiles from the
@@ -662,14 +662,16 @@ __device__ __forceinline__ void judge_finish(const FrameDesc &f, int worst, unsi
 // pick up more work instead of idling while the grid's last blocks finish.
 // A gated launch (f.gate set) renders only if *f.gate != 0; otherwise its
 // warps take their share of tickets (tiles + one failed take each) and leave.
-// JUDGE (learned skipping): every tile whose index is judge_phase modulo
-// judge_stride is marched a second time with the exact grids and the 8-bit
-// results compared (judge_finish); a learned grid already marked wrong
-// (*learned_bad) is not used: the launch marches with the exact grids.
+// JUDGE (learned skipping): the first tickets re-march the judged tiles
+// (judge_phase modulo judge_stride) with the exact grids into f.judge8,
+// each on its own warp, so that a judged heavy tile does not double the
+// launch's longest warp; the rest render every tile.  A learned grid
+// already marked wrong (*learned_bad) is not used: the tiles march with the
+// exact grids and nothing is re-marched.  judge_compare_kernel gives the
+// verdict afterwards.
 template <int DT, bool SKIP, bool CENSUS, bool JUDGE>
 __global__ void __launch_bounds__(kThreads, JUDGE ? kJudgeBlocksPerSm : kCfgBlocksPerSm)
-    march_cfg_kernel(const __grid_constant__ FrameDesc f,
-                                                                              float4 *out32, uchar4 *out8)
+    march_cfg_kernel(const __grid_constant__ FrameDesc f, float4 *out32, uchar4 *out8)
 {
     unsigned long long nexec = 0, nlat = 0;
     const int lane = threadIdx.x & 31;
@@ -680,43 +682,65 @@ __global__ void __launch_bounds__(kThreads, JUDGE ? kJudgeBlocksPerSm : kCfgBloc
         if (lane == 0) atomicAdd(f.tickets, first ? (unsigned long long) ntiles + 1ull : 1ull);
         return;
     }
-    int worst = 0;
-    unsigned judged = 0;
     const bool exact = JUDGE && *(volatile const int *) f.learned_bad != 0;
-    // judged launches hand out the judged tiles (judge_phase modulo
-    // judge_stride) first, so that their second march is spread over the
-    // launch instead of stretching its end; the other tiles follow in order
-    const long long njudged =
-        JUDGE ? (ntiles > f.judge_phase ? (ntiles - f.judge_phase + f.judge_stride - 1) / f.judge_stride : 0) : 0;
+    const long long njudged = JUDGE ? judged_tiles(ntiles, f.judge_stride, f.judge_phase) : 0;
     for (;;) {
         unsigned long long ticket = 0;
         if (lane == 0) ticket = atomicAdd(f.tickets, 1ull);
         const long long q = (long long) (__shfl_sync(0xffffffffu, ticket, 0) - f.ticket_base);
-        if (q >= ntiles) break;
-        long long tile = q;
-        if (JUDGE) {
-            if (q < njudged) {
-                tile = q * f.judge_stride + f.judge_phase;
-            } else {
-                // the (q - njudged)-th tile that is not judged
-                const long long r = q - njudged, per = f.judge_stride - 1;
-                const long long o = r % per;
-                tile = (r / per) * f.judge_stride + (o < f.judge_phase ? o : o + 1);
-            }
+        if (q >= ntiles + njudged) break;
+        if (JUDGE && q < njudged) {
+            if (exact) continue;
+            const long long tile = q * f.judge_stride + f.judge_phase;
+            const int oi = (int) (tile / tiles_x) * 4 + (lane >> 3), oj = (int) (tile % tiles_x) * 8 + (lane & 7);
+            const int i = f.out_y + oi, j = f.out_x + oj;
+            float4 ex = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (oi < f.out_h && oj < f.out_w && i < f.vh && j < f.vw)
+                ex = ray_cfg<DT, true, false, kPair>(f, i, j, nexec, nlat, true);
+            f.judge8[q * 32 + lane] = make_uchar4(q8(ex.x), q8(ex.y), q8(ex.z), q8(ex.w));
+            continue;
         }
+        const long long tile = q - njudged;
         const int oi = (int) (tile / tiles_x) * 4 + (lane >> 3), oj = (int) (tile % tiles_x) * 8 + (lane & 7);
         pixel_cfg<DT, SKIP, CENSUS, kPair>(f, oi, oj, out32, out8, nexec, nlat, exact);
-        if (JUDGE && !exact && q < njudged) {
-            const int i = f.out_y + oi, j = f.out_x + oj;
-            if (oi < f.out_h && oj < f.out_w && i < f.vh && j < f.vw) {
-                const float4 ex = ray_cfg<DT, true, false, kPair>(f, i, j, nexec, nlat, true);
-                worst = max(worst, q8_diff(out8, out32, (long long) oi * f.out_w + oj, ex));
+    }
+    if (CENSUS) count_exec(f, nexec, nlat);
+}
+
+// The verdict of a learned-skip frame: each warp compares one judged tile's
+// exact re-march (judge8) with the stored frame (out8, or out32 quantised).
+__global__ void judge_compare_kernel(JudgeArgs a, const uchar4 *judge8, const uchar4 *out8, const float4 *out32,
+                                     int out_x, int out_y, int out_w, int out_h, int vw, int vh, int stride,
+                                     int phase)
+{
+    const int lane = threadIdx.x & 31;
+    const int tiles_x = (out_w + 7) >> 3;
+    const long long njudged = judged_tiles((long long) tiles_x * ((out_h + 3) >> 2), stride, phase);
+    const bool known_bad = *(volatile const int *) a.learned_bad != 0;
+    int worst = 0;
+    unsigned judged = 0;
+    if (!known_bad)
+        for (long long q = (long long) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < njudged;
+             q += (long long) gridDim.x * (blockDim.x >> 5)) {
+            const long long tile = q * stride + phase;
+            const int oi = (int) (tile / tiles_x) * 4 + (lane >> 3), oj = (int) (tile % tiles_x) * 8 + (lane & 7);
+            if (oi < out_h && oj < out_w && out_y + oi < vh && out_x + oj < vw) {
+                const uchar4 e = judge8[q * 32 + lane];
+                const long long o = (long long) oi * out_w + oj;
+                uchar4 v;
+                if (out8) {
+                    v = out8[o];
+                } else {
+                    const float4 c = out32[o];
+                    v = make_uchar4(q8(c.x), q8(c.y), q8(c.z), q8(c.w));
+                }
+                const int d = max(max(abs((int) v.x - (int) e.x), abs((int) v.y - (int) e.y)),
+                                  max(abs((int) v.z - (int) e.z), abs((int) v.w - (int) e.w)));
+                worst = max(worst, d);
                 judged++;
             }
         }
-    }
-    if (JUDGE) judge_finish(f, worst, judged, exact);
-    if (CENSUS) count_exec(f, nexec, nlat);
+    judge_finish(a, worst, judged, known_bad);
 }
 
 // Sample-rate roofline: the CONFIG sampler (trilinear reconstruction, LUT
@@ -785,16 +809,20 @@ cudaError_t launch_dt(const FrameDesc &f, float4 *o32, uchar4 *o8, cudaStream_t 
         bool skip = false;
         for (int k = 0; k < f.nb; k++) skip |= f.b[k].empty != nullptr;
         const bool judge = f.judge != nullptr;
-        if (judge && (!skip || f.census || f.judge_stride < 1 || f.judge_phase < 0 || f.judge_phase >= f.judge_stride))
+        if (judge && (!skip || f.census || !f.judge8 || f.judge_stride < 1 || f.judge_phase < 0 ||
+                      f.judge_phase >= f.judge_stride))
             return cudaErrorInvalidValue;
         auto kern = f.census ? (skip ? march_cfg_kernel<DT, true, true, false> : march_cfg_kernel<DT, false, true, false>)
                     : judge  ? march_cfg_kernel<DT, true, false, true>
                     : skip   ? march_cfg_kernel<DT, true, false, false>
                              : march_cfg_kernel<DT, false, false, false>;
         const int blocks = persistent_grid(kern, 0);
-        // every tile is taken once and every warp ends on one failed take
+        // every tile (and, judged, every re-march) is taken once and every
+        // warp ends on one failed take
+        const long long ntiles = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2);
         if (warps_launched)
-            *warps_launched = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2) + (long long) blocks * (kThreads / 32);
+            *warps_launched = ntiles + (judge ? judged_tiles(ntiles, f.judge_stride, f.judge_phase) : 0) +
+                              (long long) blocks * (kThreads / 32);
         kern<<<blocks, kThreads, 0, s>>>(f, o32, o8);
         return cudaGetLastError();
     }
@@ -908,6 +936,23 @@ cudaError_t launch_sample_peak(const FrameDesc &f, int steps, float4 *out, long 
 int sample_peak_threads()
 {
     return persistent_grid(sample_peak_kernel<IVR_F32>, 0) * kThreads;
+}
+
+cudaError_t launch_judge_compare(const FrameDesc &f, const uchar4 *out8, const float4 *out32, cudaStream_t s)
+{
+    const long long ntiles = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2);
+    const long long nj = judged_tiles(ntiles, f.judge_stride, f.judge_phase);
+    const long long blocks = nj > 0 ? (nj + 7) / 8 : 1;  // a warp per judged tile
+    JudgeArgs a{f.judge, f.judge_reject, f.learned_bad, f.judge_tol};
+    judge_compare_kernel<<<(unsigned) (blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, s>>>(
+        a, f.judge8, out8, out32, f.out_x, f.out_y, f.out_w, f.out_h, f.vw, f.vh, f.judge_stride, f.judge_phase);
+    return cudaGetLastError();
+}
+
+long long judge_scratch_bytes(const FrameDesc &f)
+{
+    const long long ntiles = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2);
+    return judged_tiles(ntiles, f.judge_stride, f.judge_phase) * 32 * (long long) sizeof(uchar4);
 }
 
 cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaStream_t s, long long *warps)
