@@ -328,10 +328,11 @@ int ivr_server_listen(ivr_server *server, int port, int volume, int tf, int *bou
  *   grid: a cell is transparent when y + margin <= 0.
  * A view with skip = IVR_SKIP_LEARNED renders with that grid and, in the
  * same launch, marches a rotating 1/judge_stride of its 8x4 tiles again
- * with the exact grid and compares: when some 8-bit channel differs by more
- * than judge_tol, the frame is re-rendered with the exact grid by a launch
- * gated on the verdict (the decision stays on the device) and the TF's
- * learned grid is not used again. */
+ * with the exact grid (on warps of their own); a compare kernel sets the
+ * verdict: when some 8-bit channel differs by more than judge_tol, the frame
+ * is re-rendered with the exact grid by a launch gated on the verdict (the
+ * decision stays on the device) and the TF's learned grid is not used
+ * again. */
 typedef struct ivr_mlp ivr_mlp;
 #define IVR_MLP_PARAMS 6337       /* W1[32][64] (rows 26-31 zero), b1[64], W2[64][64], b2[64], w3[64], b3 */
 #define IVR_MLP_IN 32             /* feature row width (BF16) */
