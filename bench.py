@@ -243,18 +243,24 @@ def _gen_device():
         return None
 
 
+def tile_order(args):
+    from ivr_gb300 import api
+    return api.TILES_RASTER if getattr(args, "tiles", "cost") == "raster" else api.TILES_COST
+
+
 def config_of(args, wl):
     w, h = wl["image"]
     return {"workload": args.workload, "volume": "x".join(map(str, wl["shape"][::-1])) + " " + wl["dtype"],
             "bricks": "x".join(map(str, wl["bricks"])) + " + 1-voxel halo", "image": f"{w}x{h}",
             "step_voxels": wl["step"], "early_termination_alpha": wl["term"], "skip": "16^3 macrocell grid",
             "layout": "bricks" if args.linear else "bricks + corner-packed copies",
+            "tile_order": "costliest first (estimated)" if getattr(args, "tiles", "cost") == "cost" else "row order",
             "tf": "256-entry RGBA FP32 ramp", "l2": "inputs larger than L2 (volume resident, > 129 MB)",
             "parallelism": f"replicas x{args.gpus}"}
 
 
 def run_batch(args):
-    """configs[3]: one batch of 64 views x 4 TFs per step."""
+    """The batched workload: one batch of 64 views x 4 TFs per step."""
     import torch
     from ivr_gb300 import api, synth
     from ivr_gb300.state import orbit_state
@@ -316,7 +322,7 @@ def run_batch(args):
 
 
 def run_serve(args, quiet=False):
-    """configs[4]: the steering server under Poisson load."""
+    """The serving workload: the steering server under Poisson load."""
     import torch
     from ivr_gb300 import api, serve, synth
     torch.cuda.set_device(0)
@@ -378,7 +384,7 @@ def run_serve(args, quiet=False):
 
 
 def run_learned(args, quiet=False):
-    """configs[2]: learned skipping against the plain march and the exact grid."""
+    """The learned-skip workload: learned skipping against the plain march and the exact grid."""
     import torch
     from ivr_gb300 import api, synth
     from ivr_gb300.state import orbit_state
@@ -443,7 +449,8 @@ def run_learned(args, quiet=False):
         for t, (tf, st) in enumerate(zip(tfs, states)):
             for m, skip in methods.items():
                 p = api.config_params(step=L["step"], term_alpha=L["term"], skip=skip,
-                                      judge_stride=getattr(args, "judge_stride", 0) or L["judge_stride"])
+                                      judge_stride=getattr(args, "judge_stride", 0) or L["judge_stride"],
+                                      tiles=tile_order(args))
                 view = vw[m].set(v, st, p)
                 # first frame of a new TF: includes building its grid
                 torch.cuda.synchronize()
@@ -500,7 +507,9 @@ def run_learned(args, quiet=False):
         "training": {"samples": n, "epochs": L["epochs"], "batch_rows": L["batch_rows"],
                      "loss_first": float(losses[0]), "loss_last": float(losses[-1]), "features_s": t_feat,
                      "train_s": t_train, "margin": margin, "recall_of_transparent_cells": recall},
-        "gpu_launches": L["tfs"] * (L["frames"] + 1) * 4,
+        # per TF and frame: plain 1; grid 1; learned 3 (march, compare, gated
+        # fallback); the cost order adds 2 to the grid and learned frames
+        "gpu_launches": L["tfs"] * (L["frames"] + 1) * (9 if tile_order(args) == api.TILES_COST else 5),
         "clocks": clk.summary(),
     }
     for m in methods:
@@ -617,6 +626,8 @@ def main():
     ap.add_argument("--serve-batch", type=int, default=0)
     ap.add_argument("--serve-rate", default="", help="per-client request rate range lo,hi (req/s)")
     ap.add_argument("--judge-stride", type=int, default=0, help="learned skipping: judge 1 in this many tiles")
+    ap.add_argument("--tiles", default="cost", choices=["cost", "raster"],
+                    help="tile order of the skipping launches: costliest first, or row order")
     ap.add_argument("--linear", action="store_true",
                     help="render from the bricks themselves, without the corner-packed copies")
     ap.add_argument("--no-extras", action="store_true",
@@ -654,7 +665,7 @@ def main():
     ctx = api.Context(local)
     v = ctx.load_volume(vol).bricks(*wl["bricks"], overlap=1).quads(not args.linear)
     tf = ctx.transfer_function().set_lut(lut, 0, lut_scale(wl), api.TF_F2B)
-    params = api.config_params(step=wl["step"], term_alpha=wl["term"], skip=True)
+    params = api.config_params(step=wl["step"], term_alpha=wl["term"], skip=True, tiles=tile_order(args))
     view = ctx.view()
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
@@ -764,7 +775,7 @@ def main():
                              "frac_of_sample_roofline": p_exec / (p_ms / 1000.0) / 1e9 / sample_peak,
                              "ms_per_frame": p_ms / 3,
                              "note": "the march without skipping (the plain method) on 3 of the views"},
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * (3 if tile_order(args) == api.TILES_COST else 1),  # + cost and order kernels
             "clocks": clk.summary(),
         }
         if not args.no_cpu_baseline and world == 1:

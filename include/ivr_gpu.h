@@ -89,6 +89,12 @@ typedef enum { IVR_ORDER_CENTER = 0, IVR_ORDER_AXIS = 1 } ivr_order;
  * IVR_SKIP_LEARNED: the grid the volume's learned predictor gives
  * (ivr_volume_set_mlp), every frame judged against the exact grid. */
 typedef enum { IVR_SKIP_NONE = 0, IVR_SKIP_GRID = 1, IVR_SKIP_LEARNED = 2 } ivr_skip;
+/* The order in which a CONFIG launch hands its 8x4 pixel tiles to warps.
+ * IVR_TILES_COST (with a skipping grid): costliest first, by an estimate
+ * from a walk of each tile's corner rays over the macrocell grid, so that the
+ * launch does not end on a long tile drawn late.  The order never changes
+ * a pixel. */
+typedef enum { IVR_TILES_RASTER = 0, IVR_TILES_COST = 1 } ivr_tile_order;
 
 /* How a frame is sampled.
  * REF: the reference's sampling exactly (ray.c): ray-parameter step 0.001,
@@ -107,6 +113,7 @@ typedef struct ivr_render_params {
     int tilew, tileh;  /* viewport rounded down to multiples (argv[11..12]) */
     int judge_stride;  /* IVR_SKIP_LEARNED: judge 1 in judge_stride 8x4 tiles, rotating */
     int judge_tol;     /* IVR_SKIP_LEARNED: largest 8-bit channel difference accepted */
+    int tile_order;    /* ivr_tile_order (CONFIG) */
 } ivr_render_params;
 
 /* Per-frame geometry ivr_set_view computed, for callers that composite or

@@ -31,6 +31,7 @@ class RenderParams(ctypes.Structure):
         ("tileh", ctypes.c_int),
         ("judge_stride", ctypes.c_int),
         ("judge_tol", ctypes.c_int),
+        ("tile_order", ctypes.c_int),
     ]
 
 

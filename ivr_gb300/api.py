@@ -23,6 +23,8 @@ CM_BASE, CM_RAINBOW, CM_MEDICAL, CM_SEISMIC, CM_JET, CM_NOMAP = 0, 1, 2, 3, 4, -
 PRESET_REF, PRESET_CONFIG = 0, 1
 ORDER_CENTER, ORDER_AXIS = 0, 1
 SKIP_NONE, SKIP_GRID, SKIP_LEARNED = 0, 1, 2
+# ivr_tile_order: the order a CONFIG launch hands out its 8x4 tiles
+TILES_RASTER, TILES_COST = 0, 1
 MLP_PARAMS, MLP_IN, MLP_TRANSPARENT = _lib.MLP_PARAMS, _lib.MLP_IN, _lib.MLP_TRANSPARENT
 
 
@@ -39,10 +41,12 @@ def ref_params(tile=(1, 1)) -> RenderParams:
 
 
 def config_params(step=0.5, term_alpha=0.99, skip=True, tile=(1, 1), judge_stride=16,
-                  judge_tol=1) -> RenderParams:
+                  judge_tol=1, tiles=TILES_COST) -> RenderParams:
     """Benchmark sampling: true trilinear, ``step`` voxels, early termination.
     ``skip``: True/False for the exact grid or none, or a SKIP_* value
-    (SKIP_LEARNED judges 1 in ``judge_stride`` tiles at ``judge_tol``)."""
+    (SKIP_LEARNED judges 1 in ``judge_stride`` tiles at ``judge_tol``).
+    ``tiles``: TILES_COST hands out the costliest tiles first (with a
+    skipping grid), TILES_RASTER in row order; the image is the same."""
     p = RenderParams()
     _lib.load().ivr_params_config(ctypes.byref(p))
     p.step = step
@@ -50,6 +54,7 @@ def config_params(step=0.5, term_alpha=0.99, skip=True, tile=(1, 1), judge_strid
     p.skip = (SKIP_GRID if skip else SKIP_NONE) if isinstance(skip, bool) else int(skip)
     p.tilew, p.tileh = tile
     p.judge_stride, p.judge_tol = judge_stride, judge_tol
+    p.tile_order = int(tiles)
     return p
 
 

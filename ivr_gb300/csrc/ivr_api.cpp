@@ -71,6 +71,8 @@ void delete_grid(ivr_volume *v, ivr_volume::TfGrid *g)
 {
     for (size_t k = 0; k < g->dist.size(); k++)
         if (g->dist[k]) dev_free(v->ctx, g->dist[k], mc_cells(v->bricks[k]));
+    for (size_t k = 0; k < g->opac.size(); k++)
+        if (g->opac[k]) dev_free(v->ctx, g->opac[k], mc_cells(v->bricks[k]));
     if (g->ev) cudaEventDestroy(g->ev);
     if (g->built) cudaEventDestroy(g->built);
     if (g->h_reject) cudaFreeHost(g->h_reject);
@@ -188,6 +190,8 @@ int valid_params(ivr_ctx *c, const ivr_render_params *p)
             return fail(c, IVR_ERR_INVALID, "judge_stride must be in [1, 2^20]");
         if (p->judge_tol < 0 || p->judge_tol > 255) return fail(c, IVR_ERR_INVALID, "judge_tol must be in [0, 255]");
     }
+    if (p->tile_order != IVR_TILES_RASTER && p->tile_order != IVR_TILES_COST)
+        return fail(c, IVR_ERR_INVALID, "unknown tile_order %d", p->tile_order);
     return IVR_OK;
 }
 
@@ -221,6 +225,7 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, bool learned, cuda
     } else {
         g = new ivr_volume::TfGrid();
         g->dist.assign(v->bricks.size(), nullptr);
+        g->opac.assign(v->bricks.size(), nullptr);
         int rc = IVR_OK;
         if (cudaEventCreateWithFlags(&g->ev, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&g->built, cudaEventDisableTiming) != cudaSuccess ||
@@ -230,8 +235,10 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, bool learned, cuda
             rc = IVR_ERR_CUDA;
         }
         if (rc == IVR_OK) rc = dev_alloc(c, sizeof(int), (void **) &g->d_bad);
-        for (size_t k = 0; k < v->bricks.size() && rc == IVR_OK; k++)
+        for (size_t k = 0; k < v->bricks.size() && rc == IVR_OK; k++) {
             rc = dev_alloc(c, mc_cells(v->bricks[k]), (void **) &g->dist[k]);
+            if (rc == IVR_OK) rc = dev_alloc(c, mc_cells(v->bricks[k]), (void **) &g->opac[k]);
+        }
         if (rc) {
             delete_grid(v, g);
             return rc == IVR_ERR_CUDA ? fail(c, rc, "events for a distance field") : rc;
@@ -246,6 +253,14 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, bool learned, cuda
     g->rejected = false;
     *(volatile int *) g->h_reject = 0;  // no launch that reads it is pending
     CK(c, cudaMemsetAsync(g->d_bad, 0, sizeof(int), s));
+    for (size_t k = 0; k < v->bricks.size(); k++) {
+        const HostBrick &b = v->bricks[k];
+        if (zero_alpha)
+            CK(c, cudaMemsetAsync(g->opac[k], 0, mc_cells(b), s));
+        else
+            CK(c, launch_cell_opacity(b.mc_minmax, b.mcx, b.mcy, b.mcz, tf->d_aprefix, tf->n, tf->off, tf->scale,
+                                      g->opac[k], s));
+    }
     if (zero_alpha) {
         for (size_t k = 0; k < v->bricks.size(); k++) CK(c, cudaMemsetAsync(g->dist[k], kDistCap, mc_cells(v->bricks[k]), s));
     } else if (learned) {
@@ -311,6 +326,7 @@ int frame_for(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single
     f.judge_reject = nullptr;
     f.learned_bad = nullptr;
     f.judge8 = nullptr;
+    f.perm = nullptr;
     if (view->p.skip != IVR_SKIP_NONE && view->p.preset == IVR_PRESET_CONFIG) {
         // a learned grid comes with the exact one (the judge's and the
         // fallback's), unless the judge has rejected it: then only the exact
@@ -330,7 +346,10 @@ int frame_for(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single
         if (built) *built |= ebuilt;
         *grid = learned ? lg : eg;
         if (learned) *exact = eg;
-        for (int k = 0; k < f.nb; k++) f.b[k].empty = (*grid)->dist[k];
+        for (int k = 0; k < f.nb; k++) {
+            f.b[k].empty = (*grid)->dist[k];
+            f.b[k].opac = (*grid)->opac[k];
+        }
     }
     return IVR_OK;
 }
@@ -353,6 +372,36 @@ int launch_view(ivr_view *view, FrameDesc &f, float *o32, uint8_t *o8, cudaStrea
         return cuda_fail(c, e, "march launch");
     }
     view->ticket_base += (unsigned long long) used;
+    return IVR_OK;
+}
+
+// IVR_TILES_COST: the launch's tile permutation, costliest first, into
+// the view's buffers (grown to the window's tile count); sets f.perm.
+int order_tiles(ivr_view *view, FrameDesc &f, cudaStream_t s)
+{
+    ivr_ctx *c = view->ctx;
+    const long long ntiles = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2);
+    if (!view->d_tile_counts) {
+        int rc = dev_alloc(c, sizeof(int) * 128, (void **) &view->d_tile_counts);
+        if (rc) return rc;
+    }
+    if (view->tile_cap < ntiles) {
+        dev_free(c, view->d_tile_perm, sizeof(int) * (size_t) view->tile_cap);
+        dev_free(c, view->d_tile_key, (size_t) view->tile_cap);
+        view->d_tile_perm = nullptr;
+        view->d_tile_key = nullptr;
+        view->tile_cap = 0;
+        int rc = dev_alloc(c, sizeof(int) * (size_t) ntiles, (void **) &view->d_tile_perm);
+        if (rc == IVR_OK) rc = dev_alloc(c, (size_t) ntiles, (void **) &view->d_tile_key);
+        if (rc) {
+            dev_free(c, view->d_tile_perm, sizeof(int) * (size_t) ntiles);
+            view->d_tile_perm = nullptr;
+            return rc;
+        }
+        view->tile_cap = ntiles;
+    }
+    CK(c, launch_tile_order(f, view->d_tile_key, view->d_tile_counts, view->d_tile_perm, s));
+    f.perm = view->d_tile_perm;
     return IVR_OK;
 }
 
@@ -394,6 +443,10 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
         }
         f.judge8 = view->d_judge8;
     }
+    if (!touched && grid && view->p.tile_order == IVR_TILES_COST) {
+        rc = order_tiles(view, f, s);
+        if (rc) return rc;
+    }
     rc = launch_view(view, f, o32, o8, s);
     if (rc) return rc;
     if (judged) {
@@ -427,6 +480,7 @@ void ivr_params_ref(ivr_render_params *p)
     p->tileh = 1;
     p->judge_stride = 16;
     p->judge_tol = 1;
+    p->tile_order = IVR_TILES_RASTER;
 }
 
 void ivr_params_config(ivr_render_params *p)
@@ -442,6 +496,7 @@ void ivr_params_config(ivr_render_params *p)
     p->tileh = 1;
     p->judge_stride = 16;
     p->judge_tol = 1;
+    p->tile_order = IVR_TILES_COST;
 }
 
 int ivr_create(int device, size_t budget, ivr_ctx **out)
@@ -749,6 +804,7 @@ int ivr_tf_free(ivr_tf *t)
     if (!t) return IVR_ERR_INVALID;
     dev_free(t->ctx, t->d_lut, sizeof(float4) * (size_t) t->cap);
     dev_free(t->ctx, t->d_nzprefix, sizeof(int) * (size_t) (t->cap + 1));
+    dev_free(t->ctx, t->d_aprefix, sizeof(double) * (size_t) (t->cap + 1));
     delete t;
     return IVR_OK;
 }
@@ -765,12 +821,16 @@ int ivr_tf_set_lut(ivr_tf *t, const float *rgba, int n, int off, float scale, in
     if (n > t->cap) {
         dev_free(c, t->d_lut, sizeof(float4) * (size_t) t->cap);
         dev_free(c, t->d_nzprefix, sizeof(int) * (size_t) (t->cap + 1));
+        dev_free(c, t->d_aprefix, sizeof(double) * (size_t) (t->cap + 1));
         t->d_lut = nullptr;
         t->d_nzprefix = nullptr;
+        t->d_aprefix = nullptr;
         t->cap = 0;
         int rc = dev_alloc(c, sizeof(float4) * (size_t) n, (void **) &t->d_lut);
         if (rc) return rc;
         rc = dev_alloc(c, sizeof(int) * (size_t) (n + 1), (void **) &t->d_nzprefix);
+        if (rc) return rc;
+        rc = dev_alloc(c, sizeof(double) * (size_t) (n + 1), (void **) &t->d_aprefix);
         if (rc) return rc;
         t->cap = n;
     }
@@ -781,9 +841,14 @@ int ivr_tf_set_lut(ivr_tf *t, const float *rgba, int n, int off, float scale, in
     if (n > 0) {
         t->host.assign(rgba, rgba + 4 * (size_t) n);
         std::vector<int> pre((size_t) n + 1, 0);
-        for (int i = 0; i < n; i++) pre[i + 1] = pre[i] + (rgba[4 * i + 3] != 0.0f ? 1 : 0);
+        std::vector<double> apre((size_t) n + 1, 0.0);
+        for (int i = 0; i < n; i++) {
+            pre[i + 1] = pre[i] + (rgba[4 * i + 3] != 0.0f ? 1 : 0);
+            apre[i + 1] = apre[i] + (double) rgba[4 * i + 3];
+        }
         CK(c, cudaMemcpy(t->d_lut, rgba, sizeof(float4) * (size_t) n, cudaMemcpyHostToDevice));
         CK(c, cudaMemcpy(t->d_nzprefix, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice));
+        CK(c, cudaMemcpy(t->d_aprefix, apre.data(), sizeof(double) * apre.size(), cudaMemcpyHostToDevice));
     }
     t->serial = ++c->tf_serial;
     return IVR_OK;
@@ -840,6 +905,9 @@ int ivr_view_free(ivr_view *v)
     dev_free(v->ctx, v->d_tickets, sizeof(unsigned long long));
     dev_free(v->ctx, v->d_judge, sizeof(JudgeWords));
     dev_free(v->ctx, v->d_judge8, v->judge_bytes);
+    dev_free(v->ctx, v->d_tile_perm, sizeof(int) * (size_t) v->tile_cap);
+    dev_free(v->ctx, v->d_tile_key, (size_t) v->tile_cap);
+    dev_free(v->ctx, v->d_tile_counts, sizeof(int) * 128);
     delete v;
     return IVR_OK;
 }

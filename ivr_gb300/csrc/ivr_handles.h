@@ -42,6 +42,7 @@ struct ivr_volume {
         unsigned mlp_serial;          // learned: the predictor's parameter version
         unsigned long long last_use;  // ctx grid_clock
         std::vector<uint8_t *> dist;  // per brick
+        std::vector<uint8_t *> opac;  // per brick: DevBrick::opac (the exact rule's)
         cudaEvent_t ev;               // after the last launch that read it
         cudaEvent_t built;            // after its build
         // learned grids: d_bad (device) is nonzero once a judged frame was
@@ -70,6 +71,7 @@ struct ivr_tf {
     float scale = 1.0f;
     float4 *d_lut = nullptr;
     int *d_nzprefix = nullptr;
+    double *d_aprefix = nullptr;  // prefix sums of the entries' opacities
     int cap = 0;
     std::vector<float> host;
     unsigned serial = 0;
@@ -92,6 +94,11 @@ struct ivr_view {
     uchar4 *d_judge8 = nullptr;
     size_t judge_bytes = 0;
     unsigned long long judge_frame = 0;     // rotates the sampled tiles
+    // IVR_TILES_COST: the tile permutation and its scratch (tile_cap tiles)
+    int *d_tile_perm = nullptr;
+    uint8_t *d_tile_key = nullptr;
+    int *d_tile_counts = nullptr;           // 128 ints
+    long long tile_cap = 0;
 };
 
 struct ivr_batch {

@@ -33,6 +33,9 @@ struct DevBrick {
     const void *quad;       // corner-packed copy or null: element (j, i, k),
                             // j < nx-1, i < ny-1, holds the voxels (j, i),
                             // (j+1, i), (j, i+1), (j+1, i+1) of slab k
+    const uint8_t *opac;    // per macrocell: 255 sqrt(mean LUT opacity over
+                            // its value range) -- the tile cost estimate's
+                            // input; or null
 };
 
 // Learned-skip judge words of a view (device).  maxdiff and warps_done are
@@ -87,6 +90,7 @@ struct FrameDesc {
                                      // render with the exact grids
     int judge_stride, judge_phase, judge_tol;
     uchar4 *judge8;                  // the judged tiles' exact re-march, 32 pixels each
+    const int *perm;                 // CONFIG: ticket n renders tile perm[n] (null: n)
     int order[kMaxBricks];   // near -> far
     DevBrick b[kMaxBricks];
     const uint8_t *exact[kMaxBricks];  // the exact grids (judged launches)
@@ -169,8 +173,14 @@ int sample_peak_threads();
 cudaError_t launch_judge_compare(const FrameDesc &f, const uchar4 *out8, const float4 *out32, cudaStream_t s);
 // bytes of f.judge8 a judged launch of f writes
 long long judge_scratch_bytes(const FrameDesc &f);
+// the CONFIG tile order of f, costliest first, into perm (ntiles ints) with
+// key (ntiles bytes) and counts (128 ints) as scratch
+cudaError_t launch_tile_order(const FrameDesc &f, uint8_t *key, int *counts, int *perm, cudaStream_t s);
 // transparent-radius relaxation of a flag grid (kDistCap or 0 per cell)
 cudaError_t launch_dist_relax(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s);
+// per macrocell 255 sqrt(mean LUT opacity over its value range) (DevBrick::opac)
+cudaError_t launch_cell_opacity(const float *mc, int mcx, int mcy, int mcz, const double *aprefix, int lut_n,
+                                int lut_off, float lut_scale, uint8_t *opac, cudaStream_t s);
 // batched CONFIG frames of one volume dtype; *ticket must be zero at launch
 cudaError_t launch_batch(int dtype, int variant, const BatchHeader *hdr, const BatchItem *items,
                          unsigned long long *ticket, cudaStream_t s);

@@ -158,6 +158,24 @@ __global__ void empty_kernel(const float *mc, int ncell, const int *nzprefix, in
     }
 }
 
+// Per cell, 255 sqrt(mean LUT opacity over the entries its voxel range
+// [min, max] indexes) -- the input of the tile cost estimate; the square
+// root keeps small opacities apart.  aprefix[i] = sum of the opacities of
+// entries [0, i).
+__global__ void cell_opacity_kernel(const float *mc, int ncell, const double *aprefix, int lut_n, int lut_off,
+                                    float lut_scale, uint8_t *opac)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
+        int lo = (int) (mc[2 * c] * lut_scale) - lut_off;
+        int hi = (int) (mc[2 * c + 1] * lut_scale) - lut_off;
+        lo = min(max(lo, 0), lut_n - 1);
+        hi = min(max(hi, lo), lut_n - 1);
+        const double mean = (aprefix[hi + 1] - aprefix[lo]) / (double) (hi - lo + 1);
+        const float q = sqrtf(fminf(fmaxf((float) mean, 0.0f), 1.0f)) * 255.0f + 0.5f;
+        opac[c] = (uint8_t) min((int) q, 255);
+    }
+}
+
 // One relaxation step of the Chebyshev distance (in cells) from each
 // transparent cell to the nearest opaque one: d = min(cap, 1 + min over the
 // 26 neighbours), 0 for opaque cells; cells outside the grid count as
@@ -372,6 +390,14 @@ cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const
     const int ncell = mcx * mcy * mcz;
     empty_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mc, ncell, nzprefix, lut_n, lut_off, lut_scale, empty);
     return launch_dist_relax(empty, mcx, mcy, mcz, s);
+}
+
+cudaError_t launch_cell_opacity(const float *mc, int mcx, int mcy, int mcz, const double *aprefix, int lut_n,
+                                int lut_off, float lut_scale, uint8_t *opac, cudaStream_t s)
+{
+    const int ncell = mcx * mcy * mcz;
+    cell_opacity_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mc, ncell, aprefix, lut_n, lut_off, lut_scale, opac);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_dist_relax(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s)

@@ -604,6 +604,146 @@ __device__ __forceinline__ float4 pixel_cfg(const FrameDesc &f, int oi, int oj, 
     return acc;
 }
 
+// Estimated cost of one CONFIG ray, in samples: a walk over the bricks'
+// macrocell grids front to back, cell by cell, with no volume reads.  A
+// transparent cube (the grid's distance field) costs one step, as the
+// march's leap over it does; an opaque cell costs the lattice points it
+// holds, and its mean LUT opacity (b.opac) lowers the ray's estimated
+// transmittance, so that the walk stops about where early termination
+// would.  Only the order of tiles depends on it, never a pixel.
+__device__ float ray_cost(const FrameDesc &f, int i, int j)
+{
+    bool any = false;
+    for (int k = 0; k < f.nb; k++) any |= in_rect(f.b[k], i, j);
+    if (!any) return 0.0f;
+    const float u = f.left + ((float) j + 0.5f) * f.du;
+    const float v = f.bottom + ((float) i + 0.5f) * f.dv;
+    const float dx = f.ctm[0] * u + f.ctm[1] * v + f.ctm[2] * f.eyen;
+    const float dy = f.ctm[3] * u + f.ctm[4] * v + f.ctm[5] * f.eyen;
+    const float dz = f.ctm[6] * u + f.ctm[7] * v + f.ctm[8] * f.eyen;
+    const float idx = 1.0f / dx, idy = 1.0f / dy, idz = 1.0f / dz;
+    float tin, tout;
+    if (!ray_box_cfg(f.gdconst, f.origx, f.origy, f.origz, dx, dy, dz, idx, idy, idz, tin, tout)) return 0.0f;
+    const float t0 = tin > 0.0f ? tin : 0.0f;
+    const float dt = f.step / sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+    if (!(dt > 0.0f)) return 0.0f;
+    const float idt = 1.0f / dt;
+    const float ox = f.origx, oy = f.origy, oz = f.origz;
+    // log2 of the transmittance where the march stops
+    const float lstop = f.term_alpha < 1.0f ? __log2f(1.0f - f.term_alpha) : -FLT_MAX;
+    float lt = 0.0f, cost = 0.0f;
+    for (int s = 0; s < f.nb; s++) {
+        const int k = f.order[s];
+        if (f.single >= 0 && k != f.single) continue;
+        const DevBrick &b = f.b[k];
+        if (!in_rect(b, i, j)) continue;
+        float ta, tb;
+        if (!ray_box_cfg(b.dconst, ox, oy, oz, dx, dy, dz, idx, idy, idz, ta, tb)) continue;
+        float t = fmaxf(ta, t0);
+        if (b.empty == nullptr || b.opac == nullptr) {
+            cost += fmaxf(tb - t, 0.0f) * idt;
+            continue;
+        }
+        for (int it = 0; it < 4096 && t < tb; it++) {
+            // the cell a quarter step past t (the march's index arithmetic)
+            const float tm = fmaf(0.25f, dt, t);
+            const int cj = min(max((int) floorf((fmaf(dx, tm, ox) - b.bminx) * b.icx), 0), b.nx - 2) / kCell;
+            const int ci = min(max((int) floorf((fmaf(dy, tm, oy) - b.bminy) * b.icy), 0), b.ny - 2) / kCell;
+            const int ck = min(max((int) floorf((fmaf(dz, tm, oz) - b.bminz) * b.icz), 0), b.nz - 2) / kCell;
+            const long long c = ((long long) ck * b.mcy + ci) * b.mcx + cj;
+            const int r = b.empty[c];
+            const int oq = b.opac[c];
+            const int rr = max(r, 1);
+            const float tx = dx > 0.0f ? (fmaf((float) (cj + rr), b.mcwx, b.bminx) - ox) * idx
+                             : dx < 0.0f ? (fmaf((float) (cj - rr + 1), b.mcwx, b.bminx) - ox) * idx : FLT_MAX;
+            const float ty = dy > 0.0f ? (fmaf((float) (ci + rr), b.mcwy, b.bminy) - oy) * idy
+                             : dy < 0.0f ? (fmaf((float) (ci - rr + 1), b.mcwy, b.bminy) - oy) * idy : FLT_MAX;
+            const float tz = dz > 0.0f ? (fmaf((float) (ck + rr), b.mcwz, b.bminz) - oz) * idz
+                             : dz < 0.0f ? (fmaf((float) (ck - rr + 1), b.mcwz, b.bminz) - oz) * idz : FLT_MAX;
+            float te = fminf(fminf(tx, ty), fminf(tz, tb));
+            if (!(te > t)) te = t + dt;
+            if (r != 0) {
+                cost += 1.0f;
+            } else {
+                const float n = (te - t) * idt;
+                const float a = (float) (oq * oq) * (1.0f / 65025.0f) * f.alpha;
+                if (a > 0.0f) {
+                    const float la = __log2f(1.0f - fminf(a, 0.999f));  // per sample, < 0
+                    const float need = (lstop - lt) / la;
+                    if (need <= n) return cost + need;
+                    lt = fmaf(n, la, lt);
+                }
+                cost += n;
+            }
+            t = te;
+        }
+    }
+    return cost;
+}
+
+constexpr int kCostKeys = 64;  // quarter-octave buckets of the tile cost
+
+// Tile costs: four threads per 8x4 tile walk its corner rays; the tile's
+// key is the quarter-octave of the largest, counted per key in counts[0..63].
+__global__ void tile_cost_kernel(const __grid_constant__ FrameDesc f, uint8_t *key, int *counts, long long ntiles)
+{
+    __shared__ int hist[kCostKeys];
+    for (int t = threadIdx.x; t < kCostKeys; t += blockDim.x) hist[t] = 0;
+    __syncthreads();
+    const long long g = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    const long long tile = g >> 2;
+    const int corner = (int) (g & 3);
+    const int tiles_x = (f.out_w + 7) >> 3;
+    float cost = 0.0f;
+    if (tile < ntiles) {
+        const int oi = min((int) (tile / tiles_x) * 4 + (corner >> 1) * 3, f.out_h - 1);
+        const int oj = min((int) (tile % tiles_x) * 8 + (corner & 1) * 7, f.out_w - 1);
+        const int i = f.out_y + oi, j = f.out_x + oj;
+        if (i < f.vh && j < f.vw) cost = ray_cost(f, i, j);
+    }
+    cost = fmaxf(cost, __shfl_xor_sync(0xffffffffu, cost, 1));
+    cost = fmaxf(cost, __shfl_xor_sync(0xffffffffu, cost, 2));
+    if (tile < ntiles && corner == 0) {
+        const int kq = min(max((int) (__log2f(cost + 1.0f) * 4.0f), 0), kCostKeys - 1);
+        key[tile] = (uint8_t) kq;
+        atomicAdd(&hist[kq], 1);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < kCostKeys; t += blockDim.x)
+        if (hist[t]) atomicAdd(&counts[t], hist[t]);
+}
+
+// The permutation, costliest key first: perm[start(key) + n] = tile, with
+// start(key) the number of tiles of larger keys.  counts[64..127] are the
+// per-key cursors (zero on entry); ties go in block order.
+__global__ void tile_scatter_kernel(const uint8_t *key, int *counts, int *perm, long long ntiles)
+{
+    __shared__ int start[kCostKeys], loc[kCostKeys], base[kCostKeys];
+    if (threadIdx.x < kCostKeys) loc[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int k = kCostKeys - 1; k >= 0; k--) {
+            start[k] = acc;
+            acc += counts[k];
+        }
+    }
+    __syncthreads();
+    const long long tile = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    int kq = 0, rank = 0;
+    if (tile < ntiles) {
+        kq = key[tile];
+        rank = atomicAdd(&loc[kq], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < kCostKeys && loc[threadIdx.x] > 0)
+        base[threadIdx.x] = atomicAdd(&counts[kCostKeys + threadIdx.x], loc[threadIdx.x]);
+    __syncthreads();
+    if (tile < ntiles) {
+        const long long pos = (long long) start[kq] + base[kq] + rank;
+        if (pos < ntiles) perm[pos] = (int) tile;
+    }
+}
+
 // What the judge's verdict needs (from the frame descriptor).
 struct JudgeArgs {
     JudgeWords *judge;
@@ -660,6 +800,7 @@ __host__ __device__ inline long long judged_tiles(long long ntiles, int stride, 
 // CONFIG kernel, persistent: every warp takes 8x4 pixel tiles from the
 // view's ticket counter until none are left, so warps that drew short rays
 // pick up more work instead of idling while the grid's last blocks finish.
+// With f.perm the n-th ticket renders tile perm[n] (costliest first).
 // A gated launch (f.gate set) renders only if *f.gate != 0; otherwise its
 // warps take their share of tickets (tiles + one failed take each) and leave.
 // JUDGE (learned skipping): the first tickets re-march the judged tiles
@@ -700,7 +841,11 @@ __global__ void __launch_bounds__(kThreads, JUDGE ? kJudgeBlocksPerSm : kCfgBloc
             f.judge8[q * 32 + lane] = make_uchar4(q8(ex.x), q8(ex.y), q8(ex.z), q8(ex.w));
             continue;
         }
-        const long long tile = q - njudged;
+        long long tile = q - njudged;
+        if (f.perm != nullptr) {
+            const long long p = f.perm[tile];
+            if (p >= 0 && p < ntiles) tile = p;  // a permutation by construction; never leave the window
+        }
         const int oi = (int) (tile / tiles_x) * 4 + (lane >> 3), oj = (int) (tile % tiles_x) * 8 + (lane & 7);
         pixel_cfg<DT, SKIP, CENSUS, kPair>(f, oi, oj, out32, out8, nexec, nlat, exact);
     }
@@ -946,6 +1091,18 @@ cudaError_t launch_judge_compare(const FrameDesc &f, const uchar4 *out8, const f
     JudgeArgs a{f.judge, f.judge_reject, f.learned_bad, f.judge_tol};
     judge_compare_kernel<<<(unsigned) (blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, s>>>(
         a, f.judge8, out8, out32, f.out_x, f.out_y, f.out_w, f.out_h, f.vw, f.vh, f.judge_stride, f.judge_phase);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile_order(const FrameDesc &f, uint8_t *key, int *counts, int *perm, cudaStream_t s)
+{
+    const long long ntiles = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2);
+    if (ntiles <= 0) return cudaSuccess;
+    if (ntiles > (1ll << 30)) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * 2 * kCostKeys, s);
+    if (e != cudaSuccess) return e;
+    tile_cost_kernel<<<(unsigned) ((ntiles * 4 + 127) / 128), 128, 0, s>>>(f, key, counts, ntiles);
+    tile_scatter_kernel<<<(unsigned) ((ntiles + 255) / 256), 256, 0, s>>>(key, counts, perm, ntiles);
     return cudaGetLastError();
 }
 

@@ -37,7 +37,7 @@ def test_record_sizes():
     from ivr_gb300._lib import FrameInfo, RenderParams
     from ivr_gb300.state import IvrState
     assert ctypes.sizeof(IvrState) == 184
-    assert ctypes.sizeof(RenderParams) == 40
+    assert ctypes.sizeof(RenderParams) == 44
     assert ctypes.sizeof(FrameInfo) == 12 + 64 * 4 + 64 * 24 + 64 * 16
     from ivr_gb300._lib import Completion, Request, ServerConfig
     assert ctypes.sizeof(Request) == 4 + 4 + 184 + 8 + 8

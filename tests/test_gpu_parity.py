@@ -345,6 +345,36 @@ def test_tiles_equal_full_frame(ctx):
     v.free()
 
 
+@pytest.mark.parametrize("size,alpha", [((96, 96), 1.0), ((83, 61), 1.0), ((83, 61), 0.0)])
+def test_cost_tile_order_renders_every_tile_once(ctx, size, alpha):
+    """TILES_COST hands the 8x4 tiles out costliest first: the same frame,
+    bit for bit, as row order, with every pixel written (the buffers start
+    at a sentinel) -- full frames and a window, with ragged edge tiles."""
+    w, h = size
+    vol = synth.blob_volume((64, 64, 64), n_blobs=8, seed=5, dtype="f32", zero_fraction=0.5, cell=8)
+    st = orbit_state(30, 20, w, h, fovy=30.0, alpha=alpha)
+    v = ctx.load_volume(vol).bricks(2, 2, 2)
+    tf = ctx.transfer_function().set_lut(synth.ramp_tf(256), 0, 1.0, api.TF_F2B)
+    got = {}
+    for order in (api.TILES_RASTER, api.TILES_COST):
+        view = ctx.view().set(v, st, api.config_params(tiles=order))
+        o32, o8 = dev_frame(h, w)
+        view.render(tf, o32.data_ptr(), o8.data_ptr())
+        t32, _ = dev_frame(h - 9, w - 13)
+        view.render_tile(tf, 13, 9, w - 13, h - 9, t32.data_ptr())
+        got[order] = (host(o32), host(o8), host(t32))
+        view.free()
+    for a, b in zip(got[api.TILES_RASTER], got[api.TILES_COST]):
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    assert not (got[api.TILES_COST][0] == -7.0).any()
+    assert not (got[api.TILES_COST][2] == -7.0).any()
+    p = api.config_params()
+    p.tile_order = 7
+    with pytest.raises(Exception):
+        ctx.view().set(v, st, p)
+    v.free()
+
+
 def test_render_host_end_to_end(ctx, oracle_mod):
     c = load_case(GOLDEN[0])
     v = load_case_volume(ctx, c)
