@@ -375,33 +375,66 @@ int launch_view(ivr_view *view, FrameDesc &f, float *o32, uint8_t *o8, cudaStrea
     return IVR_OK;
 }
 
-// IVR_TILES_COST: the launch's tile permutation, costliest first, into
-// the view's buffers (grown to the window's tile count); sets f.perm.
-int order_tiles(ivr_view *view, FrameDesc &f, cudaStream_t s)
+// IVR_TILES_COST: the launch's tile permutation, costliest first, into the
+// view's next slot (grown to the window's tile count); sets f.perm and
+// returns the slot.  Built on the view's order stream after the launches
+// that last read the slot and after the grid's build, so it overlaps the
+// tail of the frame before (in a stream capture: on s itself).
+int order_tiles(ivr_view *view, FrameDesc &f, const ivr_volume::TfGrid *grid, cudaStream_t s, int *slot)
 {
     ivr_ctx *c = view->ctx;
     const long long ntiles = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2);
-    if (!view->d_tile_counts) {
-        int rc = dev_alloc(c, sizeof(int) * 128, (void **) &view->d_tile_counts);
-        if (rc) return rc;
+    if (!view->order_stream) {
+        if (cudaStreamCreateWithFlags(&view->order_stream, cudaStreamNonBlocking) != cudaSuccess) {
+            view->order_stream = nullptr;
+            return cuda_fail(c, cudaGetLastError(), "tile order stream");
+        }
+        for (auto &o : view->tiles) {
+            CK(c, cudaEventCreateWithFlags(&o.done, cudaEventDisableTiming));
+            CK(c, cudaEventCreateWithFlags(&o.used, cudaEventDisableTiming));
+            int rc = dev_alloc(c, sizeof(int) * 128, (void **) &o.counts);
+            if (rc) return rc;
+        }
     }
     if (view->tile_cap < ntiles) {
-        dev_free(c, view->d_tile_perm, sizeof(int) * (size_t) view->tile_cap);
-        dev_free(c, view->d_tile_key, (size_t) view->tile_cap);
-        view->d_tile_perm = nullptr;
-        view->d_tile_key = nullptr;
+        for (auto &o : view->tiles) {  // cudaFree waits for the launches that read them
+            dev_free(c, o.perm, sizeof(int) * (size_t) view->tile_cap);
+            dev_free(c, o.key, (size_t) view->tile_cap);
+            o.perm = nullptr;
+            o.key = nullptr;
+        }
         view->tile_cap = 0;
-        int rc = dev_alloc(c, sizeof(int) * (size_t) ntiles, (void **) &view->d_tile_perm);
-        if (rc == IVR_OK) rc = dev_alloc(c, (size_t) ntiles, (void **) &view->d_tile_key);
-        if (rc) {
-            dev_free(c, view->d_tile_perm, sizeof(int) * (size_t) ntiles);
-            view->d_tile_perm = nullptr;
-            return rc;
+        for (auto &o : view->tiles) {
+            int rc = dev_alloc(c, sizeof(int) * (size_t) ntiles, (void **) &o.perm);
+            if (rc == IVR_OK) rc = dev_alloc(c, (size_t) ntiles, (void **) &o.key);
+            if (rc) {
+                for (auto &q : view->tiles) {
+                    dev_free(c, q.perm, q.perm ? sizeof(int) * (size_t) ntiles : 0);
+                    dev_free(c, q.key, q.key ? (size_t) ntiles : 0);
+                    q.perm = nullptr;
+                    q.key = nullptr;
+                }
+                return rc;
+            }
         }
         view->tile_cap = ntiles;
     }
-    CK(c, launch_tile_order(f, view->d_tile_key, view->d_tile_counts, view->d_tile_perm, s));
-    f.perm = view->d_tile_perm;
+    *slot = view->tile_slot;
+    view->tile_slot ^= 1;
+    ivr_view::TileOrder &o = view->tiles[*slot];
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CK(c, cudaStreamIsCapturing(s, &cap));
+    cudaStream_t os = cap == cudaStreamCaptureStatusNone ? view->order_stream : s;
+    if (os != s) {
+        if (o.used_recorded) CK(c, cudaStreamWaitEvent(os, o.used, 0));
+        CK(c, cudaStreamWaitEvent(os, grid->built, 0));
+    }
+    CK(c, launch_tile_order(f, o.key, o.counts, o.perm, os));
+    if (os != s) {
+        CK(c, cudaEventRecord(o.done, os));
+        CK(c, cudaStreamWaitEvent(s, o.done, 0));
+    }
+    f.perm = o.perm;
     return IVR_OK;
 }
 
@@ -443,21 +476,26 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
         }
         f.judge8 = view->d_judge8;
     }
+    int slot = -1;
     if (!touched && grid && view->p.tile_order == IVR_TILES_COST) {
-        rc = order_tiles(view, f, s);
+        rc = order_tiles(view, f, grid, s, &slot);
         if (rc) return rc;
     }
     rc = launch_view(view, f, o32, o8, s);
-    if (rc) return rc;
-    if (judged) {
-        CK(c, launch_judge_compare(f, (const uchar4 *) o8, (const float4 *) o32, s));
+    if (rc == IVR_OK && judged) {
+        const cudaError_t je = launch_judge_compare(f, (const uchar4 *) o8, (const float4 *) o32, s);
+        if (je != cudaSuccess) rc = cuda_fail(c, je, "judge compare launch");
         FrameDesc ff = f;
         ff.judge = nullptr;
         for (int k = 0; k < ff.nb; k++) ff.b[k].empty = exact->dist[k];
         ff.gate = &((JudgeWords *) view->d_judge)->fail;
-        rc = launch_view(view, ff, o32, o8, s);
-        if (rc) return rc;
+        if (rc == IVR_OK) rc = launch_view(view, ff, o32, o8, s);
     }
+    if (slot >= 0) {  // the slot's readers, whether or not they launched
+        CK(c, cudaEventRecord(view->tiles[slot].used, s));
+        view->tiles[slot].used_recorded = true;
+    }
+    if (rc) return rc;
     if (grid) CK(c, cudaEventRecord(grid->ev, s));
     if (exact) CK(c, cudaEventRecord(exact->ev, s));
     return IVR_OK;
@@ -905,9 +943,17 @@ int ivr_view_free(ivr_view *v)
     dev_free(v->ctx, v->d_tickets, sizeof(unsigned long long));
     dev_free(v->ctx, v->d_judge, sizeof(JudgeWords));
     dev_free(v->ctx, v->d_judge8, v->judge_bytes);
-    dev_free(v->ctx, v->d_tile_perm, sizeof(int) * (size_t) v->tile_cap);
-    dev_free(v->ctx, v->d_tile_key, (size_t) v->tile_cap);
-    dev_free(v->ctx, v->d_tile_counts, sizeof(int) * 128);
+    for (auto &o : v->tiles) {
+        dev_free(v->ctx, o.perm, sizeof(int) * (size_t) v->tile_cap);
+        dev_free(v->ctx, o.key, (size_t) v->tile_cap);
+        dev_free(v->ctx, o.counts, sizeof(int) * 128);
+        if (o.done) cudaEventDestroy(o.done);
+        if (o.used) cudaEventDestroy(o.used);
+    }
+    if (v->order_stream) {
+        cudaStreamSynchronize(v->order_stream);
+        cudaStreamDestroy(v->order_stream);
+    }
     delete v;
     return IVR_OK;
 }

@@ -94,11 +94,22 @@ struct ivr_view {
     uchar4 *d_judge8 = nullptr;
     size_t judge_bytes = 0;
     unsigned long long judge_frame = 0;     // rotates the sampled tiles
-    // IVR_TILES_COST: the tile permutation and its scratch (tile_cap tiles)
-    int *d_tile_perm = nullptr;
-    uint8_t *d_tile_key = nullptr;
-    int *d_tile_counts = nullptr;           // 128 ints
+    // IVR_TILES_COST: two slots of the tile permutation and its scratch
+    // (tile_cap tiles each), used by alternate frames.  A frame's order is
+    // built on order_stream, so that it runs in the tail of the launch
+    // before it; `used` follows the launches that read the slot.
+    struct TileOrder {
+        int *perm = nullptr;
+        uint8_t *key = nullptr;
+        int *counts = nullptr;          // 128 ints
+        cudaEvent_t done = nullptr;     // the permutation is written
+        cudaEvent_t used = nullptr;     // its readers are done (when recorded)
+        bool used_recorded = false;
+    };
+    TileOrder tiles[2];
+    int tile_slot = 0;
     long long tile_cap = 0;
+    cudaStream_t order_stream = nullptr;
 };
 
 struct ivr_batch {
