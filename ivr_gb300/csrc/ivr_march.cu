@@ -683,27 +683,34 @@ __device__ float ray_cost(const FrameDesc &f, int i, int j)
 
 constexpr int kCostKeys = 64;  // quarter-octave buckets of the tile cost
 
-// Tile costs: four threads per 8x4 tile walk its corner rays; the tile's
-// key is the quarter-octave of the largest, counted per key in counts[0..63].
+// Tile costs: kCostRays threads per 8x4 tile walk rays of it (its centre,
+// two opposite corners, or all four); the tile's key is the quarter-octave
+// of the largest, counted per key in counts[0..63].
+#ifndef IVR_COST_RAYS
+#define IVR_COST_RAYS 4
+#endif
+constexpr int kCostRays = IVR_COST_RAYS;
+static_assert(kCostRays == 1 || kCostRays == 2 || kCostRays == 4, "rays per tile: 1, 2 or 4");
 __global__ void tile_cost_kernel(const __grid_constant__ FrameDesc f, uint8_t *key, int *counts, long long ntiles)
 {
     __shared__ int hist[kCostKeys];
     for (int t = threadIdx.x; t < kCostKeys; t += blockDim.x) hist[t] = 0;
     __syncthreads();
     const long long g = (long long) blockIdx.x * blockDim.x + threadIdx.x;
-    const long long tile = g >> 2;
-    const int corner = (int) (g & 3);
+    const long long tile = g / kCostRays;
+    const int r = (int) (g % kCostRays);
     const int tiles_x = (f.out_w + 7) >> 3;
     float cost = 0.0f;
     if (tile < ntiles) {
-        const int oi = min((int) (tile / tiles_x) * 4 + (corner >> 1) * 3, f.out_h - 1);
-        const int oj = min((int) (tile % tiles_x) * 8 + (corner & 1) * 7, f.out_w - 1);
+        const int di = kCostRays == 1 ? 2 : kCostRays == 2 ? 3 * r : 3 * (r >> 1);
+        const int dj = kCostRays == 1 ? 4 : kCostRays == 2 ? 7 * r : 7 * (r & 1);
+        const int oi = min((int) (tile / tiles_x) * 4 + di, f.out_h - 1);
+        const int oj = min((int) (tile % tiles_x) * 8 + dj, f.out_w - 1);
         const int i = f.out_y + oi, j = f.out_x + oj;
         if (i < f.vh && j < f.vw) cost = ray_cost(f, i, j);
     }
-    cost = fmaxf(cost, __shfl_xor_sync(0xffffffffu, cost, 1));
-    cost = fmaxf(cost, __shfl_xor_sync(0xffffffffu, cost, 2));
-    if (tile < ntiles && corner == 0) {
+    for (int o = 1; o < kCostRays; o <<= 1) cost = fmaxf(cost, __shfl_xor_sync(0xffffffffu, cost, o));
+    if (tile < ntiles && r == 0) {
         const int kq = min(max((int) (__log2f(cost + 1.0f) * 4.0f), 0), kCostKeys - 1);
         key[tile] = (uint8_t) kq;
         atomicAdd(&hist[kq], 1);
@@ -1101,7 +1108,7 @@ cudaError_t launch_tile_order(const FrameDesc &f, uint8_t *key, int *counts, int
     if (ntiles > (1ll << 30)) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * 2 * kCostKeys, s);
     if (e != cudaSuccess) return e;
-    tile_cost_kernel<<<(unsigned) ((ntiles * 4 + 127) / 128), 128, 0, s>>>(f, key, counts, ntiles);
+    tile_cost_kernel<<<(unsigned) ((ntiles * kCostRays + 127) / 128), 128, 0, s>>>(f, key, counts, ntiles);
     tile_scatter_kernel<<<(unsigned) ((ntiles + 255) / 256), 256, 0, s>>>(key, counts, perm, ntiles);
     return cudaGetLastError();
 }
