@@ -225,8 +225,10 @@ int ivr_render_tile(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h,
 /* One brick's sub-image over the whole viewport, zero outside its rect
  * (createlocalimage(rank)). */
 int ivr_render_brick(ivr_view *view, ivr_tf *tf, int brick, float *rgba32_dev, void *stream);
-/* End to end: STATE from host memory in, RGBA8 frame to host memory out
- * (pinned staging inside; waits for the frame). */
+/* End to end: STATE from host memory in, RGBA8 frame to host memory out;
+ * waits for the frame.  Page-locked output (cudaHostAlloc, or registered)
+ * is written by the launch itself; pageable output goes through a device
+ * buffer and a copy. */
 int ivr_render_host(ivr_view *view, ivr_volume *vol, ivr_tf *tf, const ivr_state *state,
                     const ivr_render_params *p, uint8_t *rgba8_host, void *stream);
 

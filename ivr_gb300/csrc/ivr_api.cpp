@@ -56,6 +56,20 @@ void dev_free(ivr_ctx *c, void *p, size_t bytes)
     c->used -= bytes;
 }
 
+void *host_mapping(void *p, size_t n)
+{
+    if (!p || n == 0) return nullptr;
+    cudaPointerAttributes a, z;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess || cudaPointerGetAttributes(&z, (char *) p + n - 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || z.type != cudaMemoryTypeHost || !a.devicePointer || !z.devicePointer)
+        return nullptr;
+    if ((char *) z.devicePointer - (char *) a.devicePointer != (ptrdiff_t) (n - 1)) return nullptr;
+    return a.devicePointer;
+}
+
 size_t brick_bytes(const ivr_volume *v, const HostBrick &b)
 {
     return (size_t) b.lw * b.lh * b.ld * dtype_size(v->dtype);
@@ -1025,6 +1039,13 @@ int ivr_render_host(ivr_view *view, ivr_volume *vol, ivr_tf *tf, const ivr_state
     int rc = ivr_set_view(view, vol, st, p);
     if (rc) return rc;
     size_t bytes = (size_t) view->info.vw * view->info.vh * 4;
+    // page-locked output: the launch stores the frame there itself
+    if (void *direct = host_mapping(host8, bytes)) {
+        rc = ivr_render(view, tf, nullptr, (uint8_t *) direct, stream);
+        if (rc) return rc;
+        CK(c, cudaStreamSynchronize((cudaStream_t) stream));
+        return IVR_OK;
+    }
     if (bytes > c->frame8_bytes) {
         dev_free(c, c->d_frame8, c->frame8_bytes);
         c->d_frame8 = nullptr;

@@ -145,6 +145,9 @@ int dev_alloc(ivr_ctx *c, size_t bytes, void **p);
 void dev_free(ivr_ctx *c, void *p, size_t bytes);
 
 size_t brick_bytes(const ivr_volume *v, const HostBrick &b);
+// the device address of n bytes of page-locked host memory at p mapped as
+// one range, or null (pageable memory, or not one mapping)
+void *host_mapping(void *p, size_t n);
 inline size_t mc_cells(const HostBrick &b) { return (size_t) b.mcx * b.mcy * b.mcz; }
 
 // learned skipping (ivr_learn.cpp): the predictor's parameter version

@@ -381,9 +381,15 @@ def test_render_host_end_to_end(ctx, oracle_mod):
     tf = case_tf(ctx, v, c)
     view = ctx.view()
     vh, vw = c["rgba32"].shape[:2]
-    out = np.zeros((vh, vw, 4), np.uint8)
-    view.render_host(v, tf, c["state_obj"], api.ref_params(tile=c["tile"]), out)
-    assert np.array_equal(out, oracle_mod.quantize(c["rgba32"]))
+    import torch
+    # pageable (device buffer + copy) and page-locked (the launch stores
+    # into it): ivr_host_alloc and torch's pinned allocator
+    outs = [np.zeros((vh, vw, 4), np.uint8), ctx.host_frame(vh, vw),
+            torch.zeros((vh, vw, 4), dtype=torch.uint8).pin_memory().numpy()]
+    for out in outs:
+        out[...] = 7
+        view.render_host(v, tf, c["state_obj"], api.ref_params(tile=c["tile"]), out)
+        assert np.array_equal(out, oracle_mod.quantize(c["rgba32"]))
     v.free()
 
 
