@@ -746,6 +746,11 @@ def main():
         kavg = statistics.mean(kern_ms)
         peak, how = peaks()
         sample_peak = ctx.sample_peak(v.dtype, sp)
+        layouts = {}
+        for name, code in (("corner_packed", api.SAMPLER_QUADS), ("bricks", api.SAMPLER_BRICKS),
+                           ("texture_point_x8", api.SAMPLER_TEX_POINT), ("texture_filtered", api.SAMPLER_TEX_LINEAR)):
+            g, err = ctx.sample_peak_layout(v.dtype, code, sp)
+            layouts[name] = {"gsamples_per_s": g, "max_abs_sample_err": err}
         alg_bytes = touched / args.steps + w * h * 4  # compulsory volume bytes + RGBA8 out, per launch
         achieved = alg_bytes / (kavg / 1000.0) / 1e9
         traffic = profiled_traffic()
@@ -771,6 +776,10 @@ def main():
                                 "frac": executed / args.steps / (kavg / 1000.0) / 1e9 / sample_peak,
                                 "note": "executed samples/s of the render launch against ivr_sample_peak: the "
                                         "same sampler, LUT fetch and blend alone on a cache-resident brick"},
+            "sampler_layouts": dict(layouts, note="the sampler roofline through each layout of a cache-resident "
+                                    "64^3 brick: the march reads corner_packed; bricks (8 gathers) and 8 point "
+                                    "texture fetches give the same samples; one filtered texture fetch has "
+                                    "fixed-point weights (errors in volume units; values span 0-255)"),
             "plain_kernel": {"executed_gsamples_per_s": p_exec / (p_ms / 1000.0) / 1e9,
                              "frac_of_sample_roofline": p_exec / (p_ms / 1000.0) / 1e9 / sample_peak,
                              "ms_per_frame": p_ms / 3,

@@ -405,6 +405,17 @@ int ivr_view_judge_stats(ivr_view *view, ivr_judge_stats *stats);
  * every resident thread marching its own ray.  Samples per second / 1e9
  * (waits for the timing). */
 int ivr_sample_peak(ivr_ctx *ctx, int dtype, double *gsamples_per_s, void *stream);
+/* The same roofline through other layouts of the brick, for comparison:
+ * the march reads the corner-packed copies (QUADS) or the bricks themselves
+ * (BRICKS); TEX_POINT reads a 3D texture with eight point fetches and the
+ * same blend (the same value, bit for bit); TEX_LINEAR takes one
+ * hardware-filtered texture fetch, whose fixed-point weights make it
+ * inexact.  max_abs_err (nullable): the largest |sample - exact trilinear
+ * sample| over 2^20 hashed positions, in volume units. */
+typedef enum { IVR_SAMPLER_QUADS = 0, IVR_SAMPLER_BRICKS = 1, IVR_SAMPLER_TEX_POINT = 2,
+               IVR_SAMPLER_TEX_LINEAR = 3 } ivr_sampler_layout;
+int ivr_sample_peak_layout(ivr_ctx *ctx, int dtype, int layout, double *gsamples_per_s, double *max_abs_err,
+                           void *stream);
 
 /* --- compositing and output -------------------------------------------- */
 /* compositetiles (main.c:1203-1218): num sub-images of w*h RGBA floats in

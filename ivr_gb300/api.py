@@ -25,6 +25,8 @@ ORDER_CENTER, ORDER_AXIS = 0, 1
 SKIP_NONE, SKIP_GRID, SKIP_LEARNED = 0, 1, 2
 # ivr_tile_order: the order a CONFIG launch hands out its 8x4 tiles
 TILES_RASTER, TILES_COST = 0, 1
+# ivr_sampler_layout (sample-rate roofline comparisons)
+SAMPLER_QUADS, SAMPLER_BRICKS, SAMPLER_TEX_POINT, SAMPLER_TEX_LINEAR = 0, 1, 2, 3
 MLP_PARAMS, MLP_IN, MLP_TRANSPARENT = _lib.MLP_PARAMS, _lib.MLP_IN, _lib.MLP_TRANSPARENT
 
 
@@ -150,6 +152,14 @@ class Context:
         g = ctypes.c_double()
         self.check(self.lib.ivr_sample_peak(self.h, dtype, ctypes.byref(g), _vp(stream)))
         return g.value
+
+    def sample_peak_layout(self, dtype: int, layout: int, stream=None) -> tuple:
+        """(Gsamples/s, largest |sample - exact trilinear|) of the sampler
+        roofline through a SAMPLER_* layout."""
+        g, err = ctypes.c_double(), ctypes.c_double()
+        self.check(self.lib.ivr_sample_peak_layout(self.h, dtype, layout, ctypes.byref(g), ctypes.byref(err),
+                                                   _vp(stream)))
+        return g.value, err.value
 
     def quantize(self, src, dst, n: int, stream=None):
         self.check(self.lib.ivr_quantize(self.h, _vp(src), _vp(dst), n, _vp(stream)))

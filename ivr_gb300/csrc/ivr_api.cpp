@@ -1320,8 +1320,16 @@ int ivr_batch_set_variant(ivr_batch *b, int variant)
 
 int ivr_sample_peak(ivr_ctx *c, int dtype, double *gsamples_per_s, void *stream)
 {
+    return ivr_sample_peak_layout(c, dtype, IVR_SAMPLER_QUADS, gsamples_per_s, nullptr, stream);
+}
+
+int ivr_sample_peak_layout(ivr_ctx *c, int dtype, int layout, double *gsamples_per_s, double *max_abs_err,
+                           void *stream)
+{
     if (!c || !gsamples_per_s) return c ? fail(c, IVR_ERR_INVALID, "null output") : IVR_ERR_INVALID;
     if (dtype < IVR_U8 || dtype > IVR_F32) return fail(c, IVR_ERR_INVALID, "unknown dtype %d", dtype);
+    if (layout < IVR_SAMPLER_QUADS || layout > IVR_SAMPLER_TEX_LINEAR)
+        return fail(c, IVR_ERR_INVALID, "unknown sampler layout %d", layout);
     cudaStream_t s = (cudaStream_t) stream;
     // a 64^3 brick of pseudo-random values over the LUT's range, a 256-entry
     // ramp LUT, world units = voxels
@@ -1339,13 +1347,17 @@ int ivr_sample_peak(ivr_ctx *c, int dtype, double *gsamples_per_s, void *stream)
     std::vector<float4> lut(256);
     for (int i = 0; i < 256; i++) lut[i] = make_float4(i / 255.0f, 0.5f, 1.0f - i / 255.0f, 0.02f * (i / 255.0f));
     const int threads = sample_peak_threads();
-    void *d_vol = nullptr, *d_lut = nullptr, *d_out = nullptr, *d_quad = nullptr;
-    const size_t qb = quad_bytes(dtype, n, n, n);
+    void *d_vol = nullptr, *d_lut = nullptr, *d_out = nullptr, *d_quad = nullptr, *d_err = nullptr;
+    const bool quads = layout == IVR_SAMPLER_QUADS, tex = layout >= IVR_SAMPLER_TEX_POINT;
+    const size_t qb = quads ? quad_bytes(dtype, n, n, n) : 0;
     int rc = dev_alloc(c, nvox * esz, &d_vol);
-    if (rc == IVR_OK) rc = dev_alloc(c, qb, &d_quad);
+    if (rc == IVR_OK && quads) rc = dev_alloc(c, qb, &d_quad);
     if (rc == IVR_OK) rc = dev_alloc(c, sizeof(float4) * 256, &d_lut);
     if (rc == IVR_OK) rc = dev_alloc(c, sizeof(float4) * (size_t) threads, &d_out);
+    if (rc == IVR_OK) rc = dev_alloc(c, sizeof(unsigned), &d_err);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaArray_t arr = nullptr;
+    SamplerTex st{0, 0, 1.0f};
     if (rc == IVR_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
         rc = fail(c, IVR_ERR_CUDA, "events");
     if (rc == IVR_OK) {
@@ -1358,30 +1370,77 @@ int ivr_sample_peak(ivr_ctx *c, int dtype, double *gsamples_per_s, void *stream)
         f.lut_scale = dtype == IVR_U16 ? 256.0f / 65536.0f : 1.0f;
         DevBrick &b = f.b[0];
         b.data = d_vol;
-        b.quad = d_quad;  // the layout the march reads
+        b.quad = d_quad;  // null: the sampler reads the brick itself
         b.nx = b.ny = b.nz = n;
         b.icx = b.icy = b.icz = 1.0f;
         const int steps = 4096;
         long long samples = 0;
         float ms = 0.0f;
         cudaError_t e = cudaMemcpy(d_vol, host.data(), host.size(), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = launch_quads(d_vol, dtype, n, n, n, d_quad, s);
+        if (e == cudaSuccess && quads) e = launch_quads(d_vol, dtype, n, n, n, d_quad, s);
+        if (e == cudaSuccess && tex) {
+            // the brick as a 3D array; element reads for the point fetches,
+            // filtered reads (normalised for integer types) for the other
+            const cudaChannelFormatDesc cd = dtype == IVR_U8    ? cudaCreateChannelDesc<unsigned char>()
+                                             : dtype == IVR_U16 ? cudaCreateChannelDesc<unsigned short>()
+                                                                : cudaCreateChannelDesc<float>();
+            e = cudaMalloc3DArray(&arr, &cd, make_cudaExtent(n, n, n));
+            cudaMemcpy3DParms cp = {};
+            cp.srcPtr = make_cudaPitchedPtr(d_vol, n * esz, n, n);
+            cp.dstArray = arr;
+            cp.extent = make_cudaExtent(n, n, n);
+            cp.kind = cudaMemcpyDeviceToDevice;
+            if (e == cudaSuccess) e = cudaMemcpy3D(&cp);
+            cudaResourceDesc rd = {};
+            rd.resType = cudaResourceTypeArray;
+            rd.res.array.array = arr;
+            cudaTextureDesc td = {};
+            td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+            td.normalizedCoords = 0;
+            td.filterMode = cudaFilterModePoint;
+            td.readMode = cudaReadModeElementType;
+            if (e == cudaSuccess) e = cudaCreateTextureObject(&st.point, &rd, &td, nullptr);
+            td.filterMode = cudaFilterModeLinear;
+            td.readMode = dtype == IVR_F32 ? cudaReadModeElementType : cudaReadModeNormalizedFloat;
+            st.scale = dtype == IVR_U8 ? 255.0f : dtype == IVR_U16 ? 65535.0f : 1.0f;
+            if (e == cudaSuccess) e = cudaCreateTextureObject(&st.linear, &rd, &td, nullptr);
+        }
         if (e == cudaSuccess) e = cudaMemcpy(d_lut, lut.data(), sizeof(float4) * 256, cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = launch_sample_peak(f, steps, (float4 *) d_out, &samples, s);  // warm-up
+        if (e == cudaSuccess)  // warm-up
+            e = launch_sample_peak(f, layout, st, steps, (float4 *) d_out, &samples, nullptr, s);
         if (e == cudaSuccess) e = cudaEventRecord(e0, s);
-        if (e == cudaSuccess) e = launch_sample_peak(f, steps, (float4 *) d_out, &samples, s);
+        if (e == cudaSuccess) e = launch_sample_peak(f, layout, st, steps, (float4 *) d_out, &samples, nullptr, s);
         if (e == cudaSuccess) e = cudaEventRecord(e1, s);
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-        if (e != cudaSuccess) rc = cuda_fail(c, e, "sample-rate roofline");
-        else *gsamples_per_s = (double) samples / (ms * 1e-3) / 1e9;
+        unsigned err_bits = 0;
+        if (max_abs_err) {
+            if (e == cudaSuccess) e = cudaMemsetAsync(d_err, 0, sizeof(unsigned), s);
+            if (e == cudaSuccess) e = launch_sample_peak(f, layout, st, 0, nullptr, &samples, (unsigned *) d_err, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&err_bits, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        }
+        if (e != cudaSuccess) {
+            rc = cuda_fail(c, e, "sample-rate roofline");
+        } else {
+            *gsamples_per_s = (double) samples / (ms * 1e-3) / 1e9;
+            if (max_abs_err) {
+                float v;
+                memcpy(&v, &err_bits, sizeof(v));
+                *max_abs_err = v;
+            }
+        }
     }
+    if (st.point) cudaDestroyTextureObject(st.point);
+    if (st.linear) cudaDestroyTextureObject(st.linear);
+    if (arr) cudaFreeArray(arr);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     dev_free(c, d_vol, nvox * esz);
     dev_free(c, d_quad, qb);
     dev_free(c, d_lut, sizeof(float4) * 256);
     dev_free(c, d_out, sizeof(float4) * (size_t) threads);
+    dev_free(c, d_err, sizeof(unsigned));
     return rc;
 }
 

@@ -167,7 +167,17 @@ cudaError_t launch_march(const FrameDesc &f, float4 *out32, uchar4 *out8, cudaSt
 // the sampler alone on brick f.b[0] (sample-rate roofline): every thread
 // takes `steps` samples; *samples = threads * steps; out holds one float4 per
 // thread (sample_peak_threads())
-cudaError_t launch_sample_peak(const FrameDesc &f, int steps, float4 *out, long long *samples, cudaStream_t s);
+// 3D textures of the sample-rate roofline's brick (point and hardware
+// filtered); scale turns the filtered fetch back into volume units
+struct SamplerTex {
+    cudaTextureObject_t point, linear;
+    float scale;
+};
+// the sampler roofline through an ivr_sampler_layout: samples/s launch into
+// out (when set) and the largest sample error against the exact sampler
+// into *err as float bits (when set)
+cudaError_t launch_sample_peak(const FrameDesc &f, int layout, const SamplerTex &tex, int steps, float4 *out,
+                               long long *samples, unsigned *err, cudaStream_t s);
 int sample_peak_threads();
 // the verdict of a learned-skip frame rendered by a judged launch of f
 cudaError_t launch_judge_compare(const FrameDesc &f, const uchar4 *out8, const float4 *out32, cudaStream_t s);

@@ -900,9 +900,33 @@ __global__ void judge_compare_kernel(JudgeArgs a, const uchar4 *judge8, const uc
 // termination or divergence -- over a brick small enough to stay in L1/L2.
 // Each thread marches its own ray of `steps` samples, 0.5 voxel apart, from
 // a start that neighbouring lanes share up to a voxel, as in an 8x4 tile.
-template <int DT>
+// One sample of the roofline's brick through a sampler layout: the
+// march's own sampler (corner-packed copy, or the brick itself when b.quad
+// is null), or a 3D texture of the brick -- eight point fetches blended as
+// fetch_cfg does (the same value, bit for bit), or one hardware-filtered
+// fetch (fixed-point weights).
+template <int DT, int LAYOUT>
+__device__ __forceinline__ float sample_layout(const DevBrick &b, const SamplerTex &t, float x, float y, float z)
+{
+    if (LAYOUT == IVR_SAMPLER_QUADS || LAYOUT == IVR_SAMPLER_BRICKS) return sample_cfg<DT>(b, x, y, z);
+    const CellPos c = cell_cfg(b, x, y, z);
+    if (LAYOUT == IVR_SAMPLER_TEX_LINEAR)
+        return tex3D<float>(t.linear, (float) c.j + c.fx + 0.5f, (float) c.i + c.fy + 0.5f,
+                            (float) c.k + c.fz + 0.5f) * t.scale;
+    using T = typename VoxT<DT>::T;
+    const float x0 = (float) c.j + 0.5f, y0 = (float) c.i + 0.5f, z0 = (float) c.k + 0.5f;
+    const float x1 = x0 + 1.0f, y1 = y0 + 1.0f, z1 = z0 + 1.0f;
+    const float c00 = lerpf((float) tex3D<T>(t.point, x0, y0, z0), (float) tex3D<T>(t.point, x1, y0, z0), c.fx);
+    const float c10 = lerpf((float) tex3D<T>(t.point, x0, y1, z0), (float) tex3D<T>(t.point, x1, y1, z0), c.fx);
+    const float c01 = lerpf((float) tex3D<T>(t.point, x0, y0, z1), (float) tex3D<T>(t.point, x1, y0, z1), c.fx);
+    const float c11 = lerpf((float) tex3D<T>(t.point, x0, y1, z1), (float) tex3D<T>(t.point, x1, y1, z1), c.fx);
+    return lerpf(lerpf(c00, c10, c.fy), lerpf(c01, c11, c.fy), c.fz);
+}
+
+template <int DT, int LAYOUT>
 __global__ void __launch_bounds__(kThreads, kCfgBlocksPerSm) sample_peak_kernel(const __grid_constant__ FrameDesc f,
-                                                                                int steps, float4 *out)
+                                                                                SamplerTex tex, int steps,
+                                                                                float4 *out)
 {
     const DevBrick &b = f.b[0];
     const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -921,7 +945,7 @@ __global__ void __launch_bounds__(kThreads, kCfgBlocksPerSm) sample_peak_kernel(
     const float loz = b.bminz + 1.0f / b.icz, hiz = b.bminz + (sz - 1.0f) / b.icz;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     for (int i = 0; i < steps; i++) {
-        const float s = sample_cfg<DT>(b, x, y, z);
+        const float s = sample_layout<DT, LAYOUT>(b, tex, x, y, z);
         const float4 e = lut_at(f, (int) (s * f.lut_scale) - f.lut_off);
         const float wgt = (1.0f - acc.w) * (e.w * f.alpha);
         acc.x = fmaf(wgt, e.x, acc.x);
@@ -937,6 +961,26 @@ __global__ void __launch_bounds__(kThreads, kCfgBlocksPerSm) sample_peak_kernel(
         z = z < loz ? 2.0f * loz - z : (z > hiz ? 2.0f * hiz - z : z);
     }
     out[gid] = acc;
+}
+
+// The largest |layout sample - exact trilinear sample (the brick itself)|
+// over npos hashed positions of the brick, as float bits into *err.
+template <int DT, int LAYOUT>
+__global__ void sample_err_kernel(const __grid_constant__ FrameDesc f, SamplerTex tex, int npos, unsigned *err)
+{
+    const DevBrick &b = f.b[0];
+    DevBrick ref = b;
+    ref.quad = nullptr;
+    float worst = 0.0f;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npos; p += gridDim.x * blockDim.x) {
+        unsigned h = (unsigned) p * 2654435761u + 12345u;
+        const float ux = (float) ((h = h * 1664525u + 1013904223u) >> 8) / 16777216.0f * (float) (b.nx - 1);
+        const float uy = (float) ((h = h * 1664525u + 1013904223u) >> 8) / 16777216.0f * (float) (b.ny - 1);
+        const float uz = (float) ((h = h * 1664525u + 1013904223u) >> 8) / 16777216.0f * (float) (b.nz - 1);
+        const float x = b.bminx + ux / b.icx, y = b.bminy + uy / b.icy, z = b.bminz + uz / b.icz;
+        worst = fmaxf(worst, fabsf(sample_layout<DT, LAYOUT>(b, tex, x, y, z) - sample_cfg<DT>(ref, x, y, z)));
+    }
+    atomicMax(err, __float_as_uint(worst));  // non-negative floats order as their bits
 }
 
 template <typename K>
@@ -1063,31 +1107,49 @@ cudaError_t launch_batch(int dtype, int variant, const BatchHeader *hdr, const B
     }
 }
 
-cudaError_t launch_sample_peak(const FrameDesc &f, int steps, float4 *out, long long *samples, cudaStream_t s)
+template <int DT, int LAYOUT>
+cudaError_t launch_sample_layout(const FrameDesc &f, const SamplerTex &tex, int steps, float4 *out,
+                                 long long *samples, unsigned *err, cudaStream_t s)
 {
-    int blocks = 0;
-    switch (f.dtype) {
-    case IVR_U8:
-        blocks = persistent_grid(sample_peak_kernel<IVR_U8>, 0);
-        sample_peak_kernel<IVR_U8><<<blocks, kThreads, 0, s>>>(f, steps, out);
-        break;
-    case IVR_U16:
-        blocks = persistent_grid(sample_peak_kernel<IVR_U16>, 0);
-        sample_peak_kernel<IVR_U16><<<blocks, kThreads, 0, s>>>(f, steps, out);
-        break;
-    case IVR_F32:
-        blocks = persistent_grid(sample_peak_kernel<IVR_F32>, 0);
-        sample_peak_kernel<IVR_F32><<<blocks, kThreads, 0, s>>>(f, steps, out);
-        break;
+    auto kern = sample_peak_kernel<DT, LAYOUT>;
+    const int blocks = persistent_grid(kern, 0);
+    if (out) {
+        kern<<<blocks, kThreads, 0, s>>>(f, tex, steps, out);
+        *samples = (long long) blocks * kThreads * steps;
+    }
+    if (err) sample_err_kernel<DT, LAYOUT><<<256, 256, 0, s>>>(f, tex, 1 << 20, err);
+    return cudaGetLastError();
+}
+
+template <int DT>
+cudaError_t launch_sample_dt(const FrameDesc &f, int layout, const SamplerTex &tex, int steps, float4 *out,
+                             long long *samples, unsigned *err, cudaStream_t s)
+{
+    switch (layout) {
+    case IVR_SAMPLER_QUADS: return launch_sample_layout<DT, IVR_SAMPLER_QUADS>(f, tex, steps, out, samples, err, s);
+    case IVR_SAMPLER_BRICKS: return launch_sample_layout<DT, IVR_SAMPLER_BRICKS>(f, tex, steps, out, samples, err, s);
+    case IVR_SAMPLER_TEX_POINT:
+        return launch_sample_layout<DT, IVR_SAMPLER_TEX_POINT>(f, tex, steps, out, samples, err, s);
+    case IVR_SAMPLER_TEX_LINEAR:
+        return launch_sample_layout<DT, IVR_SAMPLER_TEX_LINEAR>(f, tex, steps, out, samples, err, s);
     default: return cudaErrorInvalidValue;
     }
-    *samples = (long long) blocks * kThreads * steps;
-    return cudaGetLastError();
+}
+
+cudaError_t launch_sample_peak(const FrameDesc &f, int layout, const SamplerTex &tex, int steps, float4 *out,
+                               long long *samples, unsigned *err, cudaStream_t s)
+{
+    switch (f.dtype) {
+    case IVR_U8: return launch_sample_dt<IVR_U8>(f, layout, tex, steps, out, samples, err, s);
+    case IVR_U16: return launch_sample_dt<IVR_U16>(f, layout, tex, steps, out, samples, err, s);
+    case IVR_F32: return launch_sample_dt<IVR_F32>(f, layout, tex, steps, out, samples, err, s);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 int sample_peak_threads()
 {
-    return persistent_grid(sample_peak_kernel<IVR_F32>, 0) * kThreads;
+    return persistent_grid(sample_peak_kernel<IVR_F32, IVR_SAMPLER_QUADS>, 0) * kThreads;
 }
 
 cudaError_t launch_judge_compare(const FrameDesc &f, const uchar4 *out8, const float4 *out32, cudaStream_t s)

@@ -433,3 +433,19 @@ def test_hbm_budget_admission(ctx):
         with pytest.raises(IvrError) as e:
             small.load_volume(np.zeros((128, 128, 128), np.uint8))  # 2 MiB does not
         assert e.value.code == -3
+
+
+@pytest.mark.parametrize("dtype", [api.U8, api.U16, api.F32], ids=["u8", "u16", "f32"])
+def test_sampler_layouts(ctx, dtype):
+    """The sample-rate roofline through each layout: the march's two
+    (corner-packed copies, the bricks) and a 3D texture read by eight point
+    fetches give the exact trilinear sample; one hardware-filtered texture
+    fetch is off by its fixed-point weights (under 1% of the value range)."""
+    full = {api.U8: 255.0, api.U16: 65535.0, api.F32: 255.0}[dtype]
+    for layout in (api.SAMPLER_QUADS, api.SAMPLER_BRICKS, api.SAMPLER_TEX_POINT):
+        g, err = ctx.sample_peak_layout(dtype, layout)
+        assert g > 0 and err == 0.0, (layout, g, err)
+    g, err = ctx.sample_peak_layout(dtype, api.SAMPLER_TEX_LINEAR)
+    assert g > 0 and 0.0 < err < 0.01 * full
+    with pytest.raises(Exception):
+        ctx.sample_peak_layout(dtype, 4)
