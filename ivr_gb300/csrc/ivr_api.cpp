@@ -399,16 +399,26 @@ int order_tiles(ivr_view *view, FrameDesc &f, const ivr_volume::TfGrid *grid, cu
     ivr_ctx *c = view->ctx;
     const long long ntiles = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2);
     if (!view->order_stream) {
-        if (cudaStreamCreateWithFlags(&view->order_stream, cudaStreamNonBlocking) != cudaSuccess) {
-            view->order_stream = nullptr;
-            return cuda_fail(c, cudaGetLastError(), "tile order stream");
-        }
+        // all or nothing: the stream is set only once its slots are complete
+        cudaStream_t os = nullptr;
+        cudaError_t e = cudaStreamCreateWithFlags(&os, cudaStreamNonBlocking);
         for (auto &o : view->tiles) {
-            CK(c, cudaEventCreateWithFlags(&o.done, cudaEventDisableTiming));
-            CK(c, cudaEventCreateWithFlags(&o.used, cudaEventDisableTiming));
-            int rc = dev_alloc(c, sizeof(int) * 128, (void **) &o.counts);
-            if (rc) return rc;
+            if (e == cudaSuccess && !o.done) e = cudaEventCreateWithFlags(&o.done, cudaEventDisableTiming);
+            if (e == cudaSuccess && !o.used) e = cudaEventCreateWithFlags(&o.used, cudaEventDisableTiming);
         }
+        if (e != cudaSuccess) {
+            if (os) cudaStreamDestroy(os);
+            return cuda_fail(c, e, "tile order stream and events");
+        }
+        for (auto &o : view->tiles)
+            if (!o.counts) {
+                int rc = dev_alloc(c, sizeof(int) * 128, (void **) &o.counts);
+                if (rc) {
+                    cudaStreamDestroy(os);
+                    return rc;
+                }
+            }
+        view->order_stream = os;
     }
     if (view->tile_cap < ntiles) {
         for (auto &o : view->tiles) {  // cudaFree waits for the launches that read them
