@@ -170,19 +170,17 @@ __device__ __forceinline__ float lerpf(float a, float b, float t) { return fmaf(
 
 // CONFIG sampler: trilinear with voxel values at cell corners (the
 // reference's index convention; the halo sits on the high side), clamp to
-// edge.  Split in two so that the march's macrocell check can use the cell
-// coordinates of the sample it is about to take.
+// edge, at a position (ux, uy, uz) in the brick's voxel coordinates (voxel
+// (j, i, k) at u = (j, i, k)).  Split in two so that the march's macrocell
+// check can use the cell coordinates of the sample it is about to take.
 struct CellPos {
     int j, i, k;         // voxel cell, clamped to [0, n-2]
     float fx, fy, fz;    // position in it, [0, 1]
 };
 
-__device__ __forceinline__ CellPos cell_cfg(const DevBrick &b, float x, float y, float z)
+__device__ __forceinline__ CellPos cell_cfg(const DevBrick &b, float ux, float uy, float uz)
 {
     const int nx = b.nx, ny = b.ny, nz = b.nz;
-    float ux = (x - b.bminx) * b.icx;
-    float uy = (y - b.bminy) * b.icy;
-    float uz = (z - b.bminz) * b.icz;
     // clamp to edge: the coordinate to [0, n-1], the cell to [0, n-2]; then
     // the fraction u - floor(u) is exact and lies in [0, 1] (this gives the
     // same cell and fraction as clamping the cell and then the fraction)
@@ -236,9 +234,34 @@ __device__ __forceinline__ float fetch_cfg(const DevBrick &b, const CellPos &c)
 }
 
 template <int DT>
-__device__ __forceinline__ float sample_cfg(const DevBrick &b, float x, float y, float z)
+__device__ __forceinline__ float sample_cfg(const DevBrick &b, float ux, float uy, float uz)
 {
-    return fetch_cfg<DT>(b, cell_cfg(b, x, y, z));
+    return fetch_cfg<DT>(b, cell_cfg(b, ux, uy, uz));
+}
+
+// A ray's CONFIG lattice in a brick's voxel coordinates: lattice index i
+// samples u_i = fmaf(i, s, base) per axis, with s = (d * ic) * dt and
+// base = fmaf(d * ic, t0, (o - bmin) * ic) -- the point o + t_i d, t_i =
+// t0 + i dt, mapped by the brick's world-to-voxel scaling ic.  Three fmaf
+// per sample instead of the lattice parameter, the world point and its
+// mapping.
+struct VoxLattice {
+    float sx, sy, sz;
+    float bx, by, bz;
+};
+
+__device__ __forceinline__ VoxLattice vox_lattice(const DevBrick &b, float ox, float oy, float oz, float dx,
+                                                  float dy, float dz, float t0, float dt)
+{
+    const float ux = dx * b.icx, uy = dy * b.icy, uz = dz * b.icz;
+    VoxLattice L;
+    L.sx = ux * dt;
+    L.sy = uy * dt;
+    L.sz = uz * dt;
+    L.bx = fmaf(ux, t0, (ox - b.bminx) * b.icx);
+    L.by = fmaf(uy, t0, (oy - b.bminy) * b.icy);
+    L.bz = fmaf(uz, t0, (oz - b.bminz) * b.icz);
+    return L;
 }
 
 __device__ __forceinline__ float4 lut_at(const FrameDesc &f, int idx)
@@ -401,13 +424,16 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
         nlat += (unsigned long long) max(i1 - i0, 0);
         if (done) return;
     }
-    const float ox = f.origx, oy = f.origy, oz = f.origz;
     const float opac = f.alpha, term = f.term_alpha;
+    const VoxLattice L = vox_lattice(b, f.origx, f.origy, f.origz, dx, dy, dz, t0, dt);
+    // lattice steps per voxel (about 1 / L.s; the voxel's world size is the
+    // macrocell's over 16), for the exits of transparent cubes
+    const float isx = idx * idt * (b.mcwx * (1.0f / kCell)), isy = idy * idt * (b.mcwy * (1.0f / kCell)),
+                isz = idz * idt * (b.mcwz * (1.0f / kCell));
     int icheck = i0;  // next lattice index whose cell must be checked
     for (int i = i0; i < i1; i++) {
-        const float t = cfg_t(t0, dt, i);
-        const float x = fmaf(dx, t, ox), y = fmaf(dy, t, oy), z = fmaf(dz, t, oz);
-        const CellPos c0 = cell_cfg(b, x, y, z);
+        const float fi = (float) i;
+        const CellPos c0 = cell_cfg(b, fmaf(fi, L.sx, L.bx), fmaf(fi, L.sy, L.by), fmaf(fi, L.sz, L.bz));
         if (SKIP && i >= icheck) {
             // the sample's macrocell: its voxel cell (the sampler's own index
             // arithmetic) over 16
@@ -415,15 +441,16 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
             // r >= 1: the cube of cells within r-1 of this one is transparent
             const int r = empty[((long long) ck * b.mcy + ci) * b.mcx + cj];
             const int rr = max(r, 1);
-            // ray parameter where it leaves that cube (or this one opaque
-            // cell); approximate, the margins absorb its rounding
-            const float tx = dx > 0.0f ? (fmaf((float) (cj + rr), b.mcwx, b.bminx) - ox) * idx
-                             : dx < 0.0f ? (fmaf((float) (cj - rr + 1), b.mcwx, b.bminx) - ox) * idx : FLT_MAX;
-            const float ty = dy > 0.0f ? (fmaf((float) (ci + rr), b.mcwy, b.bminy) - oy) * idy
-                             : dy < 0.0f ? (fmaf((float) (ci - rr + 1), b.mcwy, b.bminy) - oy) * idy : FLT_MAX;
-            const float tz = dz > 0.0f ? (fmaf((float) (ck + rr), b.mcwz, b.bminz) - oz) * idz
-                             : dz < 0.0f ? (fmaf((float) (ck - rr + 1), b.mcwz, b.bminz) - oz) * idz : FLT_MAX;
-            const float q = fminf(fmaxf((fminf(tx, fminf(ty, tz)) - t0) * idt, 0.0f), (float) kMaxLattice);
+            // lattice index where the ray leaves that cube (or this one
+            // opaque cell), from the voxel planes of its faces; approximate,
+            // the margins absorb its rounding
+            const float qx = L.sx > 0.0f ? ((float) ((cj + rr) * kCell) - L.bx) * isx
+                             : L.sx < 0.0f ? ((float) ((cj - rr + 1) * kCell) - L.bx) * isx : FLT_MAX;
+            const float qy = L.sy > 0.0f ? ((float) ((ci + rr) * kCell) - L.by) * isy
+                             : L.sy < 0.0f ? ((float) ((ci - rr + 1) * kCell) - L.by) * isy : FLT_MAX;
+            const float qz = L.sz > 0.0f ? ((float) ((ck + rr) * kCell) - L.bz) * isz
+                             : L.sz < 0.0f ? ((float) ((ck - rr + 1) * kCell) - L.bz) * isz : FLT_MAX;
+            const float q = fminf(fmaxf(fminf(qx, fminf(qy, qz)), 0.0f), (float) kMaxLattice);
             const int iexit = (int) q;  // last lattice index at or before the exit
             if (r != 0) {
                 i = max(i, iexit - 2);  // the loop's ++ resumes at iexit - 1
@@ -437,9 +464,9 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
         // ray; sample_cfg clamps its indices, so computing it is always safe.
         if (PAIR && !CENSUS) {
             const int lim = SKIP ? min(i1, icheck) : i1;
-            const float t1 = cfg_t(t0, dt, i + 1);
+            const float f1 = fi + 1.0f;  // (float) (i + 1): i < 2^24
             const float s0 = fetch_cfg<DT>(b, c0);
-            const float s1 = sample_cfg<DT>(b, fmaf(dx, t1, ox), fmaf(dy, t1, oy), fmaf(dz, t1, oz));
+            const float s1 = sample_cfg<DT>(b, fmaf(f1, L.sx, L.bx), fmaf(f1, L.sy, L.by), fmaf(f1, L.sz, L.bz));
             const float4 e0 = lut_at(f, (int) (s0 * f.lut_scale) - f.lut_off);
             const float4 e1 = lut_at(f, (int) (s1 * f.lut_scale) - f.lut_off);
             float wgt = (1.0f - acc.w) * (e0.w * opac);
@@ -468,10 +495,7 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
         const float s = fetch_cfg<DT>(b, c0);
         if (CENSUS) {
             nexec++;
-            int j = min(max((int) floorf((x - b.bminx) * b.icx), 0), b.nx - 2) / kCell;
-            int ii = min(max((int) floorf((y - b.bminy) * b.icy), 0), b.ny - 2) / kCell;
-            int k = min(max((int) floorf((z - b.bminz) * b.icz), 0), b.nz - 2) / kCell;
-            b.touched[((long long) k * b.mcy + ii) * b.mcx + j] = 1;
+            b.touched[((long long) (c0.k / kCell) * b.mcy + c0.i / kCell) * b.mcx + c0.j / kCell] = 1;
         }
         const float4 e = lut_at(f, (int) (s * f.lut_scale) - f.lut_off);
         const float al = e.w * opac;
@@ -906,10 +930,10 @@ __global__ void judge_compare_kernel(JudgeArgs a, const uchar4 *judge8, const uc
 // fetch_cfg does (the same value, bit for bit), or one hardware-filtered
 // fetch (fixed-point weights).
 template <int DT, int LAYOUT>
-__device__ __forceinline__ float sample_layout(const DevBrick &b, const SamplerTex &t, float x, float y, float z)
+__device__ __forceinline__ float sample_layout(const DevBrick &b, const SamplerTex &t, float ux, float uy, float uz)
 {
-    if (LAYOUT == IVR_SAMPLER_QUADS || LAYOUT == IVR_SAMPLER_BRICKS) return sample_cfg<DT>(b, x, y, z);
-    const CellPos c = cell_cfg(b, x, y, z);
+    if (LAYOUT == IVR_SAMPLER_QUADS || LAYOUT == IVR_SAMPLER_BRICKS) return sample_cfg<DT>(b, ux, uy, uz);
+    const CellPos c = cell_cfg(b, ux, uy, uz);
     if (LAYOUT == IVR_SAMPLER_TEX_LINEAR)
         return tex3D<float>(t.linear, (float) c.j + c.fx + 0.5f, (float) c.i + c.fy + 0.5f,
                             (float) c.k + c.fz + 0.5f) * t.scale;
@@ -933,16 +957,16 @@ __global__ void __launch_bounds__(kThreads, kCfgBlocksPerSm) sample_peak_kernel(
     // the warp's 8x4 tile of starts, one voxel apart, at a hashed place
     const unsigned w = gid >> 5, lane = gid & 31;
     const unsigned h = w * 2654435761u;
+    // positions in the brick's voxel coordinates, as the march samples
     const float sx = (float) (b.nx - 2), sy = (float) (b.ny - 2), sz = (float) (b.nz - 2);
-    float x = b.bminx + (2.0f + (float) (h % 997u) / 997.0f * (sx - 12.0f) + (float) (lane & 7)) / b.icx;
-    float y = b.bminy + (2.0f + (float) ((h >> 10) % 991u) / 991.0f * (sy - 8.0f) + (float) (lane >> 3)) / b.icy;
-    float z = b.bminz + (2.0f + (float) ((h >> 20) % 983u) / 983.0f * (sz - 4.0f)) / b.icz;
+    float x = 2.0f + (float) (h % 997u) / 997.0f * (sx - 12.0f) + (float) (lane & 7);
+    float y = 2.0f + (float) ((h >> 10) % 991u) / 991.0f * (sy - 8.0f) + (float) (lane >> 3);
+    float z = 2.0f + (float) ((h >> 20) % 983u) / 983.0f * (sz - 4.0f);
     // half a voxel per step along a direction fixed per warp
-    const float dx = ((w & 1) ? 0.3f : -0.3f) / b.icx, dy = ((w & 2) ? 0.2f : -0.2f) / b.icy,
-                dz = ((w & 4) ? 0.35f : -0.35f) / b.icz;
-    const float lox = b.bminx + 1.0f / b.icx, hix = b.bminx + (sx - 1.0f) / b.icx;
-    const float loy = b.bminy + 1.0f / b.icy, hiy = b.bminy + (sy - 1.0f) / b.icy;
-    const float loz = b.bminz + 1.0f / b.icz, hiz = b.bminz + (sz - 1.0f) / b.icz;
+    const float dx = (w & 1) ? 0.3f : -0.3f, dy = (w & 2) ? 0.2f : -0.2f, dz = (w & 4) ? 0.35f : -0.35f;
+    const float lox = 1.0f, hix = sx - 1.0f;
+    const float loy = 1.0f, hiy = sy - 1.0f;
+    const float loz = 1.0f, hiz = sz - 1.0f;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     for (int i = 0; i < steps; i++) {
         const float s = sample_layout<DT, LAYOUT>(b, tex, x, y, z);
@@ -977,8 +1001,7 @@ __global__ void sample_err_kernel(const __grid_constant__ FrameDesc f, SamplerTe
         const float ux = (float) ((h = h * 1664525u + 1013904223u) >> 8) / 16777216.0f * (float) (b.nx - 1);
         const float uy = (float) ((h = h * 1664525u + 1013904223u) >> 8) / 16777216.0f * (float) (b.ny - 1);
         const float uz = (float) ((h = h * 1664525u + 1013904223u) >> 8) / 16777216.0f * (float) (b.nz - 1);
-        const float x = b.bminx + ux / b.icx, y = b.bminy + uy / b.icy, z = b.bminz + uz / b.icz;
-        worst = fmaxf(worst, fabsf(sample_layout<DT, LAYOUT>(b, tex, x, y, z) - sample_cfg<DT>(ref, x, y, z)));
+        worst = fmaxf(worst, fabsf(sample_layout<DT, LAYOUT>(b, tex, ux, uy, uz) - sample_cfg<DT>(ref, ux, uy, uz)));
     }
     atomicMax(err, __float_as_uint(worst));  // non-negative floats order as their bits
 }

@@ -388,14 +388,12 @@ static float sample_ref(const brick_t *b, float x, float y, float z)
 
 /* CONFIG sampler: true trilinear, voxel values at cell corners (the
  * reference's index convention, utils.c halo on the high side), clamp to
- * edge.  lerp(a,b,t) = fmaf(t, b-a, a). */
+ * edge, at (ux, uy, uz) in the brick's voxel coordinates (voxel (j, i, k)
+ * at u = (j, i, k)).  lerp(a,b,t) = fmaf(t, b-a, a). */
 static float lerpf_(float a, float b, float t) { return fmaf(t, b - a, a); }
-static float sample_cfg(const brick_t *b, float x, float y, float z)
+static float sample_cfg(const brick_t *b, float ux, float uy, float uz)
 {
     int nx = b->lw, ny = b->lh, nz = b->ld;
-    float ux = (x - b->bmin.x) * b->invcell.x;
-    float uy = (y - b->bmin.y) * b->invcell.y;
-    float uz = (z - b->bmin.z) * b->invcell.z;
     int j = clampi((int) floorf(ux), 0, nx - 2);
     int i = clampi((int) floorf(uy), 0, ny - 2);
     int k = clampi((int) floorf(uz), 0, nz - 2);
@@ -579,30 +577,38 @@ static void march_cfg(const orc_scene *sc, const brick_t *b, v3 o, v3 d, float t
     if (i1 <= i0) return;
     *nalg += i1 - i0;
     if (acc->done) return;
+    /* the lattice in the brick's voxel coordinates: index i samples
+     * u_i = fmaf(i, s, base) per axis, s = (d ic) dt, base = fmaf(d ic, t0,
+     * (o - bmin) ic) -- the point o + t_i d mapped by the brick's
+     * world-to-voxel scaling ic */
+    v3 du = {d.x * b->invcell.x, d.y * b->invcell.y, d.z * b->invcell.z};
+    v3 st = {du.x * dt, du.y * dt, du.z * dt};
+    v3 base = {fmaf(du.x, t0, (o.x - b->bmin.x) * b->invcell.x), fmaf(du.y, t0, (o.y - b->bmin.y) * b->invcell.y),
+               fmaf(du.z, t0, (o.z - b->bmin.z) * b->invcell.z)};
     for (int i = i0; i < i1; i++) {
-        float t = cfg_t(t0, dt, i);
-        float x = fmaf(d.x, t, o.x), y = fmaf(d.y, t, o.y), z = fmaf(d.z, t, o.z);
+        float ux = fmaf((float) i, st.x, base.x), uy = fmaf((float) i, st.y, base.y),
+              uz = fmaf((float) i, st.z, base.z);
         if (b->empty) {
-            float ux = (x - b->bmin.x) * b->invcell.x, uy = (y - b->bmin.y) * b->invcell.y,
-                  uz = (z - b->bmin.z) * b->invcell.z;
             int cj = clampi((int) floorf(ux), 0, b->lw - 2) / MC;
             int ci = clampi((int) floorf(uy), 0, b->lh - 2) / MC;
             int ck = clampi((int) floorf(uz), 0, b->ld - 2) / MC;
             if (b->empty[((size_t) ck * b->mcy + ci) * b->mcx + cj]) {
-                float lox = b->bmin.x + (float) (cj * MC) / b->invcell.x, hix = b->bmin.x + (float) ((cj + 1) * MC) / b->invcell.x;
-                float loy = b->bmin.y + (float) (ci * MC) / b->invcell.y, hiy = b->bmin.y + (float) ((ci + 1) * MC) / b->invcell.y;
-                float loz = b->bmin.z + (float) (ck * MC) / b->invcell.z, hiz = b->bmin.z + (float) ((ck + 1) * MC) / b->invcell.z;
-                float tx = d.x > 0.0f ? (hix - o.x) / d.x : (d.x < 0.0f ? (lox - o.x) / d.x : FLT_MAX);
-                float ty = d.y > 0.0f ? (hiy - o.y) / d.y : (d.y < 0.0f ? (loy - o.y) / d.y : FLT_MAX);
-                float tz = d.z > 0.0f ? (hiz - o.z) / d.z : (d.z < 0.0f ? (loz - o.z) / d.z : FLT_MAX);
-                float texit = fminf(tx, fminf(ty, tz));
-                float q = (texit - t0) / dt;
-                int inext = (q < (float) CFG_MAX_LATTICE ? (int) q : CFG_MAX_LATTICE) - 1;
+                /* lattice index of the exit through the cell's voxel faces
+                 * (in double); leap to one before it, so rounding never
+                 * steps over a sample outside the cell */
+                double qx = st.x > 0.0f ? ((double) ((cj + 1) * MC) - base.x) / st.x
+                          : (st.x < 0.0f ? ((double) (cj * MC) - base.x) / st.x : 1e30);
+                double qy = st.y > 0.0f ? ((double) ((ci + 1) * MC) - base.y) / st.y
+                          : (st.y < 0.0f ? ((double) (ci * MC) - base.y) / st.y : 1e30);
+                double qz = st.z > 0.0f ? ((double) ((ck + 1) * MC) - base.z) / st.z
+                          : (st.z < 0.0f ? ((double) (ck * MC) - base.z) / st.z : 1e30);
+                double q = fmin(qx, fmin(qy, qz));
+                int inext = (q < (double) CFG_MAX_LATTICE ? (int) q : CFG_MAX_LATTICE) - 1;
                 if (inext > i) i = (inext < i1 ? inext : i1) - 1;
                 continue;
             }
         }
-        float s = sample_cfg(b, x, y, z);
+        float s = sample_cfg(b, ux, uy, uz);
         (*nexec)++;
         int idx = (int) (s * sc->lut_scale) - tf->off;
         c4 e = lutat(tf, idx);
