@@ -437,23 +437,37 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
         if (SKIP && i >= icheck) {
             // the sample's macrocell: its voxel cell (the sampler's own index
             // arithmetic) over 16
-            const int cj = c0.j / kCell, ci = c0.i / kCell, ck = c0.k / kCell;
+            // (cells are never negative: the sampler clamps them)
+            const int cj = (int) ((unsigned) c0.j / kCell), ci = (int) ((unsigned) c0.i / kCell),
+                      ck = (int) ((unsigned) c0.k / kCell);
             // r >= 1: the cube of cells within r-1 of this one is transparent
-            const int r = empty[((long long) ck * b.mcy + ci) * b.mcx + cj];
+            const int r = empty[(ck * b.mcy + ci) * b.mcx + cj];
             const int rr = max(r, 1);
-            // lattice index where the ray leaves that cube (or this one
-            // opaque cell), from the voxel planes of its faces; approximate,
-            // the margins absorb its rounding
-            const float qx = L.sx > 0.0f ? ((float) ((cj + rr) * kCell) - L.bx) * isx
-                             : L.sx < 0.0f ? ((float) ((cj - rr + 1) * kCell) - L.bx) * isx : FLT_MAX;
-            const float qy = L.sy > 0.0f ? ((float) ((ci + rr) * kCell) - L.by) * isy
-                             : L.sy < 0.0f ? ((float) ((ci - rr + 1) * kCell) - L.by) * isy : FLT_MAX;
-            const float qz = L.sz > 0.0f ? ((float) ((ck + rr) * kCell) - L.bz) * isz
-                             : L.sz < 0.0f ? ((float) ((ck - rr + 1) * kCell) - L.bz) * isz : FLT_MAX;
+            // the voxel plane of the face through which the ray leaves that
+            // cube (or this one opaque cell), per axis, and the lattice index
+            // of the exit; approximate, the margins absorb its rounding
+            const float fx = (float) ((L.sx > 0.0f ? cj + rr : cj - rr + 1) * kCell);
+            const float fy = (float) ((L.sy > 0.0f ? ci + rr : ci - rr + 1) * kCell);
+            const float fz = (float) ((L.sz > 0.0f ? ck + rr : ck - rr + 1) * kCell);
+            const float qx = L.sx != 0.0f ? (fx - L.bx) * isx : FLT_MAX;
+            const float qy = L.sy != 0.0f ? (fy - L.by) * isy : FLT_MAX;
+            const float qz = L.sz != 0.0f ? (fz - L.bz) * isz : FLT_MAX;
             const float q = fminf(fmaxf(fminf(qx, fminf(qy, qz)), 0.0f), (float) kMaxLattice);
             const int iexit = (int) q;  // last lattice index at or before the exit
             if (r != 0) {
-                i = max(i, iexit - 2);  // the loop's ++ resumes at iexit - 1
+                // Leap.  Sample positions are monotone in the lattice index
+                // along each axis and sample i lies in the cube, so when the
+                // last one before the exit (iexit) is still short of every
+                // exit face, so is every sample up to it: all are in the
+                // transparent cube, and the march resumes just past the
+                // exit.  Otherwise (rounding at a face) it resumes two
+                // samples earlier, where the next check looks again.
+                const float fe = (float) iexit;
+                const float ex = fmaf(fe, L.sx, L.bx), ey = fmaf(fe, L.sy, L.by), ez = fmaf(fe, L.sz, L.bz);
+                const bool inside = (L.sx > 0.0f ? ex < fx : L.sx < 0.0f ? ex >= fx : true) &&
+                                    (L.sy > 0.0f ? ey < fy : L.sy < 0.0f ? ey >= fy : true) &&
+                                    (L.sz > 0.0f ? ez < fz : L.sz < 0.0f ? ez >= fz : true);
+                i = max(i, inside ? iexit : iexit - 2);  // the loop's ++ resumes at iexit + 1 or iexit - 1
                 continue;
             }
             icheck = iexit + 1;

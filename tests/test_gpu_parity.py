@@ -327,6 +327,32 @@ def test_config_skip_is_lossless_and_cheaper(ctx):
     v.free()
 
 
+@pytest.mark.parametrize("dtype", ["u8", "f32"])
+def test_skip_lossless_at_axis_views(ctx, dtype):
+    """Macrocell leaps along and across the axes (ray direction components
+    of zero and of both signs, views straight down an axis, and steps of
+    0.25-1 voxel): the skipping march gives the unskipped frame bit for bit
+    and executes fewer samples."""
+    vol = synth.blob_volume((72, 64, 56), n_blobs=10, seed=13, dtype=dtype, zero_fraction=0.6, cell=8)
+    lut = synth.ramp_tf(256)
+    v = ctx.load_volume(vol).bricks(2, 2, 1)
+    tf = ctx.transfer_function().set_lut(lut, 0, 1.0, api.TF_F2B)
+    for az, el, step in [(0, 0, 0.5), (90, 0, 0.25), (180, 0, 1.0), (270, 0, 0.5), (45, 0, 0.5), (0, 45, 0.5),
+                         (0, -89.5, 0.5), (135, 30, 0.75)]:
+        st = orbit_state(az, el, 64, 64, fovy=30.0, alpha=1.0)
+        outs, execd = [], []
+        for skip in (False, True):
+            view = ctx.view().set(v, st, api.config_params(step=step, skip=skip))
+            o32, _ = dev_frame(64, 64)
+            view.render(tf, o32.data_ptr())
+            outs.append(host(o32))
+            execd.append(view.census(tf)["executed"])
+            view.free()
+        assert np.array_equal(bits(outs[0]), bits(outs[1])), (az, el, step)
+        assert execd[1] < execd[0], (az, el, step)
+    v.free()
+
+
 def test_tiles_equal_full_frame(ctx):
     vol = make_config_volume((40, 40, 40), "u8", 9)
     st = orbit_state(60, -20, 80, 64, fovy=30.0, alpha=1.0)
