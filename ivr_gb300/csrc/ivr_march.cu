@@ -432,9 +432,13 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
                 isz = idz * idt * (b.mcwz * (1.0f / kCell));
     int icheck = i0;  // next lattice index whose cell must be checked
     for (int i = i0; i < i1; i++) {
-        const float fi = (float) i;
-        const CellPos c0 = cell_cfg(b, fmaf(fi, L.sx, L.bx), fmaf(fi, L.sy, L.by), fmaf(fi, L.sz, L.bz));
-        if (SKIP && i >= icheck) {
+        float fi = (float) i;
+        CellPos c0 = cell_cfg(b, fmaf(fi, L.sx, L.bx), fmaf(fi, L.sy, L.by), fmaf(fi, L.sz, L.bz));
+        // A lane leaps over transparent cubes within one iteration, until
+        // its sample lies in an opaque cell (or the brick ends), so that it
+        // samples beside the lanes that did not leap.  Every leap moves i
+        // forward and an opaque check leaves the loop, so it ends.
+        if (SKIP && i >= icheck) for (;;) {
             // the sample's macrocell: its voxel cell (the sampler's own index
             // arithmetic) over 16
             // (cells are never negative: the sampler clamps them)
@@ -467,11 +471,16 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
                 const bool inside = (L.sx > 0.0f ? ex < fx : L.sx < 0.0f ? ex >= fx : true) &&
                                     (L.sy > 0.0f ? ey < fy : L.sy < 0.0f ? ey >= fy : true) &&
                                     (L.sz > 0.0f ? ez < fz : L.sz < 0.0f ? ez >= fz : true);
-                i = max(i, inside ? iexit : iexit - 2);  // the loop's ++ resumes at iexit + 1 or iexit - 1
+                i = max(i, inside ? iexit : iexit - 2) + 1;  // iexit + 1 or iexit - 1
+                if (i >= i1) break;
+                fi = (float) i;
+                c0 = cell_cfg(b, fmaf(fi, L.sx, L.bx), fmaf(fi, L.sy, L.by), fmaf(fi, L.sz, L.bz));
                 continue;
             }
             icheck = iexit + 1;
+            break;
         }
+        if (SKIP && i >= i1) break;
         // PAIR: two samples per iteration, both samples' loads in flight
         // before either is composited.  The second is only composited when
         // it comes before the next cell check and the first did not end the
