@@ -197,6 +197,23 @@ __device__ __forceinline__ CellPos cell_cfg(const DevBrick &b, float ux, float u
     return c;
 }
 
+// Packed integer voxels without conversion instructions (which run on a
+// narrow pipe; eight per sample made the u8/u16 corner-packed sampler
+// conversion-bound): a u8 or u16 lane placed in the low mantissa bits under
+// the exponent of 2^23 is the float 2^23 + v, exactly.  lerp23 is lerpf on
+// two such values: B - A is b - a and A - 2^23 is a, both exact, so the
+// result is lerpf(a, b, t) bit for bit.  (For the brick's own voxels, one
+// load each, the conversion is cheaper than the permute and the offset.)
+__device__ __forceinline__ float off23(unsigned v, unsigned sel)
+{
+    return __int_as_float(__byte_perm(v, 0x4B000000u, sel));
+}
+__device__ __forceinline__ float lerp23(float A, float B, float t) { return fmaf(t, B - A, A - 8388608.0f); }
+// byte_perm selectors: u8 lane n of a word, u16 half n of a word, each with
+// 0x4B in the top byte and zeros between
+constexpr unsigned kU8Lane0 = 0x7540u, kU8Lane1 = 0x7541u, kU8Lane2 = 0x7542u, kU8Lane3 = 0x7543u;
+constexpr unsigned kU16Half0 = 0x7410u, kU16Half1 = 0x7432u;
+
 template <int DT>
 __device__ __forceinline__ float fetch_cfg(const DevBrick &b, const CellPos &c)
 {
@@ -209,11 +226,29 @@ __device__ __forceinline__ float fetch_cfg(const DevBrick &b, const CellPos &c)
         using V = typename VoxT<DT>::V4;
         const unsigned qx = (unsigned) nx - 1u, qs = qx * ((unsigned) ny - 1u);
         const V *e = reinterpret_cast<const V *>(b.quad) + ((unsigned) k * qs + (unsigned) i * qx + (unsigned) j);
-        const V lo = __ldg(e), hi = __ldg(e + qs);
-        c00 = lerpf((float) lo.x, (float) lo.y, fx);
-        c10 = lerpf((float) lo.z, (float) lo.w, fx);
-        c01 = lerpf((float) hi.x, (float) hi.y, fx);
-        c11 = lerpf((float) hi.z, (float) hi.w, fx);
+        if (DT == IVR_U8) {
+            // one word per element: lanes (j, i), (j+1, i), (j, i+1), (j+1, i+1)
+            const unsigned lo = __ldg(reinterpret_cast<const unsigned *>(e));
+            const unsigned hi = __ldg(reinterpret_cast<const unsigned *>(e + qs));
+            c00 = lerp23(off23(lo, kU8Lane0), off23(lo, kU8Lane1), fx);
+            c10 = lerp23(off23(lo, kU8Lane2), off23(lo, kU8Lane3), fx);
+            c01 = lerp23(off23(hi, kU8Lane0), off23(hi, kU8Lane1), fx);
+            c11 = lerp23(off23(hi, kU8Lane2), off23(hi, kU8Lane3), fx);
+        } else if (DT == IVR_U16) {
+            // two words per element, two lanes each
+            const uint2 lo = __ldg(reinterpret_cast<const uint2 *>(e));
+            const uint2 hi = __ldg(reinterpret_cast<const uint2 *>(e + qs));
+            c00 = lerp23(off23(lo.x, kU16Half0), off23(lo.x, kU16Half1), fx);
+            c10 = lerp23(off23(lo.y, kU16Half0), off23(lo.y, kU16Half1), fx);
+            c01 = lerp23(off23(hi.x, kU16Half0), off23(hi.x, kU16Half1), fx);
+            c11 = lerp23(off23(hi.y, kU16Half0), off23(hi.y, kU16Half1), fx);
+        } else {
+            const V lo = __ldg(e), hi = __ldg(e + qs);
+            c00 = lerpf((float) lo.x, (float) lo.y, fx);
+            c10 = lerpf((float) lo.z, (float) lo.w, fx);
+            c01 = lerpf((float) hi.x, (float) hi.y, fx);
+            c11 = lerpf((float) hi.z, (float) hi.w, fx);
+        }
     } else {
         // one pointer to the cell's low corner (a brick holds fewer than
         // 2^32 voxels, checked at load, so its offset fits 32 bits); the
