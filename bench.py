@@ -248,11 +248,42 @@ def tile_order(args):
     return api.TILES_RASTER if getattr(args, "tiles", "cost") == "raster" else api.TILES_COST
 
 
+def measure_cells(v, view, tf, params, states, args, o8, stream, cell):
+    """frames/s and executed samples of the timed views with the volume's
+    macrocell edge switched to `cell` (outside the headline's timed region),
+    and whether the last frame is the headline's frame bit for bit."""
+    import torch
+    sp = stream.cuda_stream
+    ref = o8.clone()
+    v.macrocell(cell)
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup):
+            view.set(v, states[k], params)
+            view.render(tf, None, o8.data_ptr(), sp)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.steps):
+            view.set(v, states[args.warmup + k], params)
+            view.render(tf, None, o8.data_ptr(), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    same = bool(torch.equal(o8, ref))
+    executed = 0
+    for st in states[args.warmup:]:
+        view.set(v, st, params)
+        executed += view.census(tf, sp)["executed"]
+    return {"fps": args.steps / (ms / 1000.0), "executed_per_frame": executed / args.steps,
+            "last_frame_equal": same}
+
+
 def config_of(args, wl):
     w, h = wl["image"]
     return {"workload": args.workload, "volume": "x".join(map(str, wl["shape"][::-1])) + " " + wl["dtype"],
             "bricks": "x".join(map(str, wl["bricks"])) + " + 1-voxel halo", "image": f"{w}x{h}",
-            "step_voxels": wl["step"], "early_termination_alpha": wl["term"], "skip": "16^3 macrocell grid",
+            "step_voxels": wl["step"], "early_termination_alpha": wl["term"],
+            "skip": f"macrocell grid of {getattr(args, 'cell', 16)}^3-voxel cells",
             "layout": "bricks" if args.linear else "bricks + corner-packed copies",
             "tile_order": "costliest first (estimated)" if getattr(args, "tiles", "cost") == "cost" else "row order",
             "tf": "256-entry RGBA FP32 ramp", "l2": "inputs larger than L2 (volume resident, > 129 MB)",
@@ -628,6 +659,8 @@ def main():
     ap.add_argument("--judge-stride", type=int, default=0, help="learned skipping: judge 1 in this many tiles")
     ap.add_argument("--tiles", default="cost", choices=["cost", "raster"],
                     help="tile order of the skipping launches: costliest first, or row order")
+    ap.add_argument("--cell", type=int, default=16,
+                    help="macrocell edge of the skipping grid in voxels (a power of two, 4-32)")
     ap.add_argument("--linear", action="store_true",
                     help="render from the bricks themselves, without the corner-packed copies")
     ap.add_argument("--no-extras", action="store_true",
@@ -663,7 +696,7 @@ def main():
     lut = synth.ramp_tf(256)
 
     ctx = api.Context(local)
-    v = ctx.load_volume(vol).bricks(*wl["bricks"], overlap=1).quads(not args.linear)
+    v = ctx.load_volume(vol).bricks(*wl["bricks"], overlap=1).quads(not args.linear).macrocell(args.cell)
     tf = ctx.transfer_function().set_lut(lut, 0, lut_scale(wl), api.TF_F2B)
     params = api.config_params(step=wl["step"], term_alpha=wl["term"], skip=True, tiles=tile_order(args))
     view = ctx.view()
@@ -751,6 +784,12 @@ def main():
                            ("texture_point_x8", api.SAMPLER_TEX_POINT), ("texture_filtered", api.SAMPLER_TEX_LINEAR)):
             g, err = ctx.sample_peak_layout(v.dtype, code, sp)
             layouts[name] = {"gsamples_per_s": g, "max_abs_sample_err": err}
+        other_cells = {}
+        if world == 1 and not args.no_extras:
+            # the same frames with another macrocell edge (same image)
+            for cell in ((8,) if args.cell != 8 else (16,)):
+                other_cells[f"{cell}^3"] = measure_cells(v, view, tf, params, states, args, o8, stream, cell)
+            v.macrocell(args.cell)
         alg_bytes = touched / args.steps + w * h * 4  # compulsory volume bytes + RGBA8 out, per launch
         achieved = alg_bytes / (kavg / 1000.0) / 1e9
         traffic = profiled_traffic()
@@ -787,6 +826,10 @@ def main():
             "gpu_launches": args.steps * (3 if tile_order(args) == api.TILES_COST else 1),  # + cost and order kernels
             "clocks": clk.summary(),
         }
+        if other_cells:
+            line["other_macrocell_edges"] = dict(other_cells, note=(
+                "the same views with the skipping grid's cells of another edge (ivr_volume_set_macrocell); "
+                "the headline uses the configuration's 16^3-voxel cells; the images are the same"))
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(wl, vol, states[args.warmup:], budget_s=args.cpu_budget)
     v.free()

@@ -177,6 +177,18 @@ int ivr_volume_gradient(ivr_volume *vol, float *grad4_dev, void *stream);
  * are the same either way.  Switching rebuilds the bricks. */
 int ivr_volume_set_quads(ivr_volume *vol, int on);
 int ivr_volume_quad_bytes(const ivr_volume *vol, size_t *bytes);  /* bytes held by the copies */
+/* Macrocell edge of the CONFIG empty-space skipping grids, in voxels: a
+ * power of two in [4, 32], 16 by default (no counterpart in the reference,
+ * which has no skipping).  Smaller cells hug the transparent regions more
+ * closely, so fewer samples are taken, at the price of more cell crossings
+ * and of grids 8x larger per halving.  The images are the same for every
+ * edge.  Switching rebuilds the bricks and drops the volume's per-TF grids;
+ * views set on the volume derive their frames again on their next render.
+ * A predictor attached with ivr_volume_set_mlp stays attached: its grids are
+ * built from the new cells (certified and judged as before), but it predicts
+ * best on the cell size it was trained on. */
+int ivr_volume_set_macrocell(ivr_volume *vol, int cell);
+int ivr_volume_macrocell(const ivr_volume *vol, int *cell);
 /* min, max and the histogram of mathutil.c:444-470 (hist may be NULL;
  * otherwise it holds hsize = (int)(max-min+1) bins). */
 int ivr_volume_minmax(ivr_volume *vol, float *mn, float *mx);

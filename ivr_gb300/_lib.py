@@ -115,6 +115,8 @@ SIGNATURES = {
     "ivr_volume_free": (_I, [_P]),
     "ivr_bricks_setup": (_I, [_P, _I, _I, _I, _I]),
     "ivr_volume_set_quads": (_I, [_P, _I]),
+    "ivr_volume_set_macrocell": (_I, [_P, _I]),
+    "ivr_volume_macrocell": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
     "ivr_volume_gradient": (_I, [_P, _P, _P]),
     "ivr_volume_quad_bytes": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
     "ivr_volume_minmax": (_I, [_P, _PF, _PF]),

@@ -183,6 +183,17 @@ class Volume:
         self.ctx.check(self.ctx.lib.ivr_volume_set_quads(self.h, int(on)))
         return self
 
+    def macrocell(self, cell: int) -> "Volume":
+        """Macrocell edge of the skipping grids in voxels (a power of two in
+        [4, 32]; 16 by default).  The images do not depend on it."""
+        self.ctx.check(self.ctx.lib.ivr_volume_set_macrocell(self.h, int(cell)))
+        return self
+
+    def macrocell_edge(self) -> int:
+        c = ctypes.c_int()
+        self.ctx.check(self.ctx.lib.ivr_volume_macrocell(self.h, ctypes.byref(c)))
+        return c.value
+
     def quad_bytes(self) -> int:
         n = ctypes.c_size_t()
         self.ctx.check(self.ctx.lib.ivr_volume_quad_bytes(self.h, ctypes.byref(n)))

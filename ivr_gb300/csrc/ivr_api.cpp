@@ -128,15 +128,17 @@ void free_bricks(ivr_volume *v)
     v->bricks.clear();
 }
 
-// macrocell grid over a brick's local voxels (cells of kCell, +1 layer)
+// macrocell grid over a brick's local voxels (cells of the volume's edge,
+// +1 layer)
 int build_macrocells(ivr_volume *v, HostBrick &b)
 {
-    b.mcx = (b.lw - 2) / kCell + 1;
-    b.mcy = (b.lh - 2) / kCell + 1;
-    b.mcz = (b.ld - 2) / kCell + 1;
+    b.cell = v->cell;
+    b.mcx = (b.lw - 2) / b.cell + 1;
+    b.mcy = (b.lh - 2) / b.cell + 1;
+    b.mcz = (b.ld - 2) / b.cell + 1;
     int rc = dev_alloc(v->ctx, mc_cells(b) * 2 * sizeof(float), (void **) &b.mc_minmax);
     if (rc) return rc;
-    CK(v->ctx, launch_macrocells(b.data, v->dtype, b.lw, b.lh, b.ld, b.mc_minmax, b.mcx, b.mcy, b.mcz, 0));
+    CK(v->ctx, launch_macrocells(b.data, v->dtype, b.lw, b.lh, b.ld, b.cell, b.mc_minmax, b.mcx, b.mcy, b.mcz, 0));
     return IVR_OK;
 }
 
@@ -148,6 +150,7 @@ int setup_bricks(ivr_volume *v, int py, int px, int pz, int overlap)
     if (v->w / px < 2 || v->h / py < 2 || v->d / pz < 2)
         return fail(c, IVR_ERR_INVALID, "bricks of %dx%dx%d voxels are too thin", v->w / px, v->h / py, v->d / pz);
     free_bricks(v);
+    v->layout++;
     int K = py * px * pz;
     v->bricks.resize(K);
     for (int r = 0; r < K; r++) {
@@ -323,6 +326,19 @@ int frame_for(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single
     const bool f2b = tf->mode == IVR_TF_F2B;
     if ((view->p.preset == IVR_PRESET_CONFIG) != f2b)
         return fail(c, IVR_ERR_UNSUPPORTED, "CONFIG preset needs IVR_TF_F2B and REF needs ids 0-5 (got %d)", tf->mode);
+    if (view->layout != view->vol->layout) {
+        // the volume's bricks were rebuilt (ivr_bricks_setup, corner-packed
+        // copies or macrocell edge switched) since ivr_set_view: derive the
+        // frame again from the view's STATE and parameters
+        ivr_volume *vol = view->vol;
+        int rc = build_frame(vol->w, vol->h, vol->d, vol->dtype, vol->bricks.data(), (int) vol->bricks.size(),
+                             view->st, view->p, view->f, view->info);
+        if (rc) {
+            view->valid = false;
+            return fail(c, rc, "view set-up failed after the volume's bricks changed");
+        }
+        view->layout = vol->layout;
+    }
     if (x < 0 || y < 0 || w < 1 || h < 1 || x + w > view->info.vw || y + h > view->info.vh)
         return fail(c, IVR_ERR_INVALID, "tile %d,%d %dx%d outside the %dx%d viewport", x, y, w, h, view->info.vw,
                     view->info.vh);
@@ -785,6 +801,24 @@ int ivr_volume_set_quads(ivr_volume *v, int on)
     return setup_bricks(v, v->py, v->px, v->pz, v->overlap);  // rebuilt with or without the copies
 }
 
+int ivr_volume_set_macrocell(ivr_volume *v, int cell)
+{
+    if (!v) return IVR_ERR_INVALID;
+    if (cell < kMinCell || cell > kMaxCell || (cell & (cell - 1)) != 0)
+        return fail(v->ctx, IVR_ERR_INVALID, "macrocell edge %d: a power of two in [%d, %d]", cell, kMinCell, kMaxCell);
+    if (v->cell == cell) return IVR_OK;
+    CK(v->ctx, cudaSetDevice(v->ctx->device));
+    v->cell = cell;
+    return setup_bricks(v, v->py, v->px, v->pz, v->overlap);  // grids rebuilt on the new cells
+}
+
+int ivr_volume_macrocell(const ivr_volume *v, int *cell)
+{
+    if (!v || !cell) return IVR_ERR_INVALID;
+    *cell = v->cell;
+    return IVR_OK;
+}
+
 int ivr_volume_quad_bytes(const ivr_volume *v, size_t *bytes)
 {
     if (!v || !bytes) return IVR_ERR_INVALID;
@@ -1010,6 +1044,7 @@ int ivr_set_view(ivr_view *view, ivr_volume *vol, const ivr_state *st, const ivr
     if (rc) return fail(c, rc, "view set-up failed (window %dx%d, tile %dx%d)", st->winwidth, st->winheight,
                         p->tilew, p->tileh);
     view->vol = vol;
+    view->layout = vol->layout;
     view->p = *p;
     view->st = *st;
     view->valid = true;
@@ -1099,8 +1134,9 @@ int ivr_census(ivr_view *view, ivr_tf *tf, unsigned long long *lattice, unsigned
             for (int cy = 0; cy < b.mcy; cy++)
                 for (int cx = 0; cx < b.mcx; cx++)
                     if (h[((size_t) cz * b.mcy + cy) * b.mcx + cx])
-                        bytes += (size_t) std::min(kCell, b.lw - cx * kCell) * std::min(kCell, b.lh - cy * kCell) *
-                                 std::min(kCell, b.ld - cz * kCell) * dtype_size(vol->dtype);
+                        bytes += (size_t) std::min(b.cell, b.lw - cx * b.cell) *
+                                 std::min(b.cell, b.lh - cy * b.cell) * std::min(b.cell, b.ld - cz * b.cell) *
+                                 dtype_size(vol->dtype);
     }
     for (size_t k = 0; k < touched.size(); k++)
         if (touched[k]) dev_free(c, touched[k], mc_cells(vol->bricks[k]));
@@ -1383,6 +1419,8 @@ int ivr_sample_peak_layout(ivr_ctx *c, int dtype, int layout, double *gsamples_p
         b.quad = d_quad;  // null: the sampler reads the brick itself
         b.nx = b.ny = b.nz = n;
         b.icx = b.icy = b.icz = 1.0f;
+        b.vwx = b.vwy = b.vwz = 1.0f;
+        b.cshift = 4;
         const int steps = 4096;
         long long samples = 0;
         float ms = 0.0f;

@@ -194,9 +194,14 @@ int build_frame(int gw, int gh, int gd, int dtype, const HostBrick *bricks, int 
         b.icy = (float) hb.ch / hb.h;
         b.icz = (float) hb.cd / hb.d;
         b.mcx = hb.mcx; b.mcy = hb.mcy; b.mcz = hb.mcz;
-        b.mcwx = (float) kCell / b.icx;
-        b.mcwy = (float) kCell / b.icy;
-        b.mcwz = (float) kCell / b.icz;
+        b.mcwx = (float) hb.cell / b.icx;
+        b.mcwy = (float) hb.cell / b.icy;
+        b.mcwz = (float) hb.cell / b.icz;
+        b.vwx = 1.0f / b.icx;
+        b.vwy = 1.0f / b.icy;
+        b.vwz = 1.0f / b.icz;
+        b.cshift = 0;
+        while ((1 << b.cshift) < hb.cell) b.cshift++;
         // pzero (main.c:616-618) and setplaneconst (ray.c:44-51)
         float pz0[6] = {hb.bminx * -1.0f, hb.bmaxx * 1.0f, hb.bminy * -1.0f,
                         hb.bmaxy * 1.0f, hb.bminz * -1.0f, hb.bmaxz * 1.0f};

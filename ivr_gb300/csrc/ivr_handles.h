@@ -30,6 +30,8 @@ struct ivr_volume {
     std::vector<ivr::HostBrick> bricks;
     int py = 1, px = 1, pz = 1, overlap = 0;
     bool quads = true;  // keep corner-packed copies of the bricks (HostBrick::quad)
+    int cell = ivr::kCell;  // macrocell edge in voxels (ivr_volume_set_macrocell)
+    unsigned layout = 0;    // counts brick rebuilds: views set before one re-derive their frame
     bool have_minmax = false;
     float vmin = 0.0f, vmax = 0.0f;
     // macrocell distance fields, one set per transfer function in use
@@ -86,6 +88,7 @@ struct ivr_view {
     ivr_render_params p{};
     ivr_state st{};
     bool valid = false;
+    unsigned layout = 0;   // the volume's brick layout the frame was derived for
     ivr::FrameDesc f{};
     ivr_frame_info info{};
     // learned-skip judge: the per-frame verdict words and running totals,

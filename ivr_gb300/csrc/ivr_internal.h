@@ -9,7 +9,8 @@
 namespace ivr {
 
 constexpr int kMaxBricks = IVR_MAX_BRICKS;
-constexpr int kCell = 16;  // macrocell edge in voxels
+constexpr int kCell = 16;  // default macrocell edge in voxels (ivr_volume_set_macrocell)
+constexpr int kMinCell = 4, kMaxCell = 32;  // the edges a volume may use: powers of two
 constexpr int kDistCap = 8;  // largest transparent radius stored per macrocell
 
 // One brick as the march kernels see it.  Geometry follows the reference's
@@ -22,6 +23,8 @@ struct DevBrick {
     float w, h, d;          // aabb.w/h/d
     float icx, icy, icz;    // CONFIG: core voxels per world unit
     float mcwx, mcwy, mcwz; // CONFIG: world size of one macrocell
+    float vwx, vwy, vwz;    // CONFIG: world size of one voxel, 1 / ic
+    int cshift;             // log2 of the macrocell edge in voxels
     float dconst[6];        // clip-plane constants of this brick
     int istrt, istop, jstrt, jstop;  // pixel rect (createlocalimage)
     float dir0x, dir0y, dir0z;       // REF: ray direction at (istrt, jstrt)
@@ -128,6 +131,7 @@ struct HostBrick {
     bool owns;          // false when it aliases the full volume
     float *mc_minmax;   // device [mcz][mcy][mcx][2]
     int mcx, mcy, mcz;
+    int cell;           // macrocell edge in voxels (a power of two)
     void *quad;         // device corner-packed copy (DevBrick::quad) or null
 };
 
@@ -140,8 +144,8 @@ cudaError_t launch_gather_brick(const void *src, int gw, int gh, int gd, void *d
 cudaError_t launch_minmax(const void *data, int dtype, long long n, float *partial, int nparts, cudaStream_t s);
 cudaError_t launch_histogram(const void *data, int dtype, long long n, float mn, int hsize, int *hist,
                              cudaStream_t s);
-cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int nz, float *mc, int mcx, int mcy,
-                              int mcz, cudaStream_t s);
+cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int nz, int cell, float *mc, int mcx,
+                              int mcy, int mcz, cudaStream_t s);
 cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const int *nzprefix, int lut_n,
                                int lut_off, float lut_scale, uint8_t *empty, cudaStream_t s);
 // per-voxel gradient (gx, gy, gz, |g|) of a w x h x d volume into out

@@ -107,15 +107,16 @@ __global__ void hist_global_kernel(const void *data, int dtype, long long n, flo
     }
 }
 
-// Macrocell min/max: cell (cx,cy,cz) spans voxels [c*16, min(c*16+16, n-1)]
-// per axis -- its 16 cells plus the +1 layer a trilinear sample in the cell
-// also reads.  One block per cell.
-__global__ void macrocell_kernel(const void *data, int dtype, int nx, int ny, int nz, float *mc, int mcx, int mcy)
+// Macrocell min/max: with edge `cell`, cell (cx,cy,cz) spans voxels
+// [c*cell, min(c*cell+cell, n-1)] per axis -- its voxel cells plus the +1
+// layer a trilinear sample in the cell also reads.  One block per cell.
+__global__ void macrocell_kernel(const void *data, int dtype, int nx, int ny, int nz, int cell, float *mc, int mcx,
+                                 int mcy)
 {
     const int cid = blockIdx.x;
     const int cx = cid % mcx, cy = (cid / mcx) % mcy, cz = cid / (mcx * mcy);
-    const int x0 = cx * kCell, y0 = cy * kCell, z0 = cz * kCell;
-    const int x1 = min(x0 + kCell, nx - 1), y1 = min(y0 + kCell, ny - 1), z1 = min(z0 + kCell, nz - 1);
+    const int x0 = cx * cell, y0 = cy * cell, z0 = cz * cell;
+    const int x1 = min(x0 + cell, nx - 1), y1 = min(y0 + cell, ny - 1), z1 = min(z0 + cell, nz - 1);
     const int ex = x1 - x0 + 1, ey = y1 - y0 + 1, ez = z1 - z0 + 1;
     float lo = FLT_MAX, hi = -FLT_MAX;
     const int tot = ex * ey * ez;
@@ -377,10 +378,10 @@ cudaError_t launch_histogram(const void *data, int dtype, long long n, float mn,
     return cudaGetLastError();
 }
 
-cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int nz, float *mc, int mcx, int mcy,
-                              int mcz, cudaStream_t s)
+cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int nz, int cell, float *mc, int mcx,
+                              int mcy, int mcz, cudaStream_t s)
 {
-    macrocell_kernel<<<mcx * mcy * mcz, 128, 0, s>>>(data, dtype, nx, ny, nz, mc, mcx, mcy);
+    macrocell_kernel<<<mcx * mcy * mcz, 128, 0, s>>>(data, dtype, nx, ny, nz, cell, mc, mcx, mcy);
     return cudaGetLastError();
 }
 

@@ -111,7 +111,7 @@ int ensure_cell_hist(ivr_volume *v, cudaStream_t s)
     for (size_t k = 0; k < v->bricks.size() && rc == IVR_OK; k++) {
         const HostBrick &b = v->bricks[k];
         rc = dev_alloc(v->ctx, mc_cells(b) * 8 * sizeof(float), (void **) &h[k]);
-        if (rc == IVR_OK && mlp_cell_hist(b.data, v->dtype, b.lw, b.lh, b.ld, b.mcx, b.mcy, b.mcz, mn, mx, h[k], s) !=
+        if (rc == IVR_OK && mlp_cell_hist(b.data, v->dtype, b.lw, b.lh, b.ld, b.cell, b.mcx, b.mcy, b.mcz, mn, mx, h[k], s) !=
                                 cudaSuccess)
             rc = fail(v->ctx, IVR_ERR_CUDA, "cell histogram launch");
     }

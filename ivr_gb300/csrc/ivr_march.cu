@@ -461,10 +461,9 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
     }
     const float opac = f.alpha, term = f.term_alpha;
     const VoxLattice L = vox_lattice(b, f.origx, f.origy, f.origz, dx, dy, dz, t0, dt);
-    // lattice steps per voxel (about 1 / L.s; the voxel's world size is the
-    // macrocell's over 16), for the exits of transparent cubes
-    const float isx = idx * idt * (b.mcwx * (1.0f / kCell)), isy = idy * idt * (b.mcwy * (1.0f / kCell)),
-                isz = idz * idt * (b.mcwz * (1.0f / kCell));
+    // lattice steps per voxel (about 1 / L.s), for the exits of transparent
+    // cubes
+    const float isx = idx * idt * b.vwx, isy = idy * idt * b.vwy, isz = idz * idt * b.vwz;
     int icheck = i0;  // next lattice index whose cell must be checked
     for (int i = i0; i < i1; i++) {
         float fi = (float) i;
@@ -475,19 +474,19 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
         // forward and an opaque check leaves the loop, so it ends.
         if (SKIP && i >= icheck) for (;;) {
             // the sample's macrocell: its voxel cell (the sampler's own index
-            // arithmetic) over 16
-            // (cells are never negative: the sampler clamps them)
-            const int cj = (int) ((unsigned) c0.j / kCell), ci = (int) ((unsigned) c0.i / kCell),
-                      ck = (int) ((unsigned) c0.k / kCell);
+            // arithmetic) over the macrocell edge (cells are never negative:
+            // the sampler clamps them)
+            const int cs = b.cshift;
+            const int cj = c0.j >> cs, ci = c0.i >> cs, ck = c0.k >> cs;
             // r >= 1: the cube of cells within r-1 of this one is transparent
             const int r = empty[(ck * b.mcy + ci) * b.mcx + cj];
             const int rr = max(r, 1);
             // the voxel plane of the face through which the ray leaves that
             // cube (or this one opaque cell), per axis, and the lattice index
             // of the exit; approximate, the margins absorb its rounding
-            const float fx = (float) ((L.sx > 0.0f ? cj + rr : cj - rr + 1) * kCell);
-            const float fy = (float) ((L.sy > 0.0f ? ci + rr : ci - rr + 1) * kCell);
-            const float fz = (float) ((L.sz > 0.0f ? ck + rr : ck - rr + 1) * kCell);
+            const float fx = (float) ((L.sx > 0.0f ? cj + rr : cj - rr + 1) << cs);
+            const float fy = (float) ((L.sy > 0.0f ? ci + rr : ci - rr + 1) << cs);
+            const float fz = (float) ((L.sz > 0.0f ? ck + rr : ck - rr + 1) << cs);
             const float qx = L.sx != 0.0f ? (fx - L.bx) * isx : FLT_MAX;
             const float qy = L.sy != 0.0f ? (fy - L.by) * isy : FLT_MAX;
             const float qz = L.sz != 0.0f ? (fz - L.bz) * isz : FLT_MAX;
@@ -553,7 +552,7 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
         const float s = fetch_cfg<DT>(b, c0);
         if (CENSUS) {
             nexec++;
-            b.touched[((long long) (c0.k / kCell) * b.mcy + c0.i / kCell) * b.mcx + c0.j / kCell] = 1;
+            b.touched[((long long) (c0.k >> b.cshift) * b.mcy + (c0.i >> b.cshift)) * b.mcx + (c0.j >> b.cshift)] = 1;
         }
         const float4 e = lut_at(f, (int) (s * f.lut_scale) - f.lut_off);
         const float al = e.w * opac;
@@ -729,9 +728,9 @@ __device__ float ray_cost(const FrameDesc &f, int i, int j)
         for (int it = 0; it < 4096 && t < tb; it++) {
             // the cell a quarter step past t (the march's index arithmetic)
             const float tm = fmaf(0.25f, dt, t);
-            const int cj = min(max((int) floorf((fmaf(dx, tm, ox) - b.bminx) * b.icx), 0), b.nx - 2) / kCell;
-            const int ci = min(max((int) floorf((fmaf(dy, tm, oy) - b.bminy) * b.icy), 0), b.ny - 2) / kCell;
-            const int ck = min(max((int) floorf((fmaf(dz, tm, oz) - b.bminz) * b.icz), 0), b.nz - 2) / kCell;
+            const int cj = min(max((int) floorf((fmaf(dx, tm, ox) - b.bminx) * b.icx), 0), b.nx - 2) >> b.cshift;
+            const int ci = min(max((int) floorf((fmaf(dy, tm, oy) - b.bminy) * b.icy), 0), b.ny - 2) >> b.cshift;
+            const int ck = min(max((int) floorf((fmaf(dz, tm, oz) - b.bminz) * b.icz), 0), b.nz - 2) >> b.cshift;
             const long long c = ((long long) ck * b.mcy + ci) * b.mcx + cj;
             const int r = b.empty[c];
             const int oq = b.opac[c];

@@ -361,15 +361,16 @@ __global__ void mlp_pack_kernel(const float *p, bf16 *w1t, bf16 *w2t, bf16 *w2)
 }
 
 // Per-cell 8-bin histogram of a brick's voxels over the volume range
-// [vmin, vmax], cells as in the macrocell grid (16 voxels plus the +1 layer).
-__global__ void cell_hist_kernel(const void *data, int dtype, int nx, int ny, int nz, int mcx, int mcy, float vmin,
-                                 float vmax, float *hist)
+// [vmin, vmax], cells as in the macrocell grid (`cell` voxels plus the +1
+// layer).
+__global__ void cell_hist_kernel(const void *data, int dtype, int nx, int ny, int nz, int cell, int mcx, int mcy,
+                                 float vmin, float vmax, float *hist)
 {
     const int cid = blockIdx.x;
     const int cx = cid % mcx, cy = (cid / mcx) % mcy, cz = cid / (mcx * mcy);
-    const int x0 = cx * kCell, y0 = cy * kCell, z0 = cz * kCell;
-    const int ex = min(x0 + kCell, nx - 1) - x0 + 1, ey = min(y0 + kCell, ny - 1) - y0 + 1,
-              ez = min(z0 + kCell, nz - 1) - z0 + 1;
+    const int x0 = cx * cell, y0 = cy * cell, z0 = cz * cell;
+    const int ex = min(x0 + cell, nx - 1) - x0 + 1, ey = min(y0 + cell, ny - 1) - y0 + 1,
+              ez = min(z0 + cell, nz - 1) - z0 + 1;
     __shared__ int sh[8];
     if (threadIdx.x < 8) sh[threadIdx.x] = 0;
     __syncthreads();
@@ -561,10 +562,10 @@ cudaError_t mlp_pack(const float *p, void *w1t, void *w2t, void *w2, cudaStream_
     return cudaGetLastError();
 }
 
-cudaError_t mlp_cell_hist(const void *data, int dtype, int nx, int ny, int nz, int mcx, int mcy, int mcz, float vmin,
-                          float vmax, float *hist, cudaStream_t s)
+cudaError_t mlp_cell_hist(const void *data, int dtype, int nx, int ny, int nz, int cell, int mcx, int mcy, int mcz,
+                          float vmin, float vmax, float *hist, cudaStream_t s)
 {
-    cell_hist_kernel<<<mcx * mcy * mcz, 128, 0, s>>>(data, dtype, nx, ny, nz, mcx, mcy, vmin, vmax, hist);
+    cell_hist_kernel<<<mcx * mcy * mcz, 128, 0, s>>>(data, dtype, nx, ny, nz, cell, mcx, mcy, vmin, vmax, hist);
     return cudaGetLastError();
 }
 

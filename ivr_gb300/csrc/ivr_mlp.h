@@ -43,8 +43,8 @@ cudaError_t mlp_train_step(const MlpDev &w, const void *X, const float *T, const
 cudaError_t mlp_adam(float *p, float *m, float *v, const float *grad, float lr, int step, void *w1t, void *w2t,
                      void *w2, cudaStream_t s);
 cudaError_t mlp_pack(const float *p, void *w1t, void *w2t, void *w2, cudaStream_t s);
-cudaError_t mlp_cell_hist(const void *data, int dtype, int nx, int ny, int nz, int mcx, int mcy, int mcz, float vmin,
-                          float vmax, float *hist, cudaStream_t s);
+cudaError_t mlp_cell_hist(const void *data, int dtype, int nx, int ny, int nz, int cell, int mcx, int mcy, int mcz,
+                          float vmin, float vmax, float *hist, cudaStream_t s);
 cudaError_t mlp_cell_features(const float *mc, const float *hist, int ncell, float vmin, float vmax,
                               const float *knots_dev, const float4 *lut, int lut_n, int lut_off, float lut_scale,
                               void *X, float *targets, cudaStream_t s);

@@ -120,19 +120,19 @@ def knots(lut, off, scale, vmin, vmax):
     return out
 
 
-def cell_grid(nx, ny, nz):
-    """Macrocell grid dims of an nx x ny x nz brick: cells of 16 voxel
-    spacings, each with its +1 layer."""
-    return (nx - 2) // CELL + 1, (ny - 2) // CELL + 1, (nz - 2) // CELL + 1
+def cell_grid(nx, ny, nz, cell=CELL):
+    """Macrocell grid dims of an nx x ny x nz brick: cells of `cell` voxel
+    spacings (16 by default), each with its +1 layer."""
+    return (nx - 2) // cell + 1, (ny - 2) // cell + 1, (nz - 2) // cell + 1
 
 
-def features(vol, lut, off, scale):
+def features(vol, lut, off, scale, cell=CELL):
     """Features (float32 holding BF16 values, [n][32]) and bounds ([n]) of
-    every macrocell of a one-brick volume, cells x fastest."""
+    every macrocell (edge `cell`) of a one-brick volume, cells x fastest."""
     v = np.asarray(vol).astype(np.float32)
     nz, ny, nx = v.shape
     vmin, vmax = np.float32(v.min()), np.float32(v.max())
-    mcx, mcy, mcz = cell_grid(nx, ny, nz)
+    mcx, mcy, mcz = cell_grid(nx, ny, nz, cell)
     kn = knots(lut, off, scale, vmin, vmax)
     inv = np.float32(1.0) / (vmax - vmin) if vmax > vmin else np.float32(0.0)
     hscale = np.float32(8.0) / (vmax - vmin) if vmax > vmin else np.float32(0.0)
@@ -142,8 +142,8 @@ def features(vol, lut, off, scale):
     for cz in range(mcz):
         for cy in range(mcy):
             for cx in range(mcx):
-                x0, y0, z0 = cx * CELL, cy * CELL, cz * CELL
-                blk = v[z0:min(z0 + CELL, nz - 1) + 1, y0:min(y0 + CELL, ny - 1) + 1, x0:min(x0 + CELL, nx - 1) + 1]
+                x0, y0, z0 = cx * cell, cy * cell, cz * cell
+                blk = v[z0:min(z0 + cell, nz - 1) + 1, y0:min(y0 + cell, ny - 1) + 1, x0:min(x0 + cell, nx - 1) + 1]
                 lo, hi = blk.min(), blk.max()
                 bins = np.clip(np.trunc((blk - vmin) * hscale).astype(np.int64), 0, 7)
                 hist = np.bincount(bins.ravel(), minlength=8).astype(np.float32) / np.float32(blk.size)

@@ -276,6 +276,50 @@ def test_a_wrong_predictor_never_reaches_the_image(ctx, scene):
         learned.free()
 
 
+def test_learned_skipping_on_8_voxel_cells(ctx):
+    """The predictor on 8^3-voxel macrocells (ivr_volume_set_macrocell):
+    features and exact bounds bitwise against the oracle on those cells, and
+    certified learned frames equal to the exact grid's, bit for bit."""
+    vol_np = synth.blob_volume((64, 64, 64), n_blobs=12, seed=6, dtype="u8", zero_fraction=0.6)
+    vol = ctx.load_volume(vol_np).macrocell(8)
+    assert vol.macrocell_edge() == 8
+    tfs, luts = [], []
+    for s in range(3):
+        lut, _ = synth.knot_tf(200 + s, zero_first=True)
+        luts.append(lut)
+        tfs.append(ctx.transfer_function().set_lut(lut, 0, 1.0, api.TF_F2B))
+    mlp = ctx.mlp(21)
+    views = []
+    try:
+        for tf, lut in zip(tfs, luts):
+            X, T, n = _features(ctx, mlp, vol, tf)
+            Xo, To = M.features(vol_np, lut, 0, 1.0, cell=8)
+            assert n == len(To) == 8 ** 3
+            np.testing.assert_array_equal(_sync_cpu(X).view(np.uint16).astype(np.uint32), M.bf16_bits(Xo))
+            np.testing.assert_array_equal(_sync_cpu(T), To.astype(np.float32))
+            mlp.add_samples(vol, tf)
+        mlp.train(300, batch_rows=64, lr=3e-3, wneg=4.0)
+        margin, _ = mlp.calibrate(0.02)
+        vol.set_mlp(mlp, margin, certify=True)
+        exact, learned = ctx.view(), ctx.view()
+        views = [exact, learned]
+        for i, tf in enumerate(tfs):
+            st = orbit_state(30 + 50 * i, 10 + 5 * i, 160, 128)
+            exact.set(vol, st, api.config_params(skip=api.SKIP_GRID))
+            learned.set(vol, st, api.config_params(skip=api.SKIP_LEARNED, judge_stride=1))
+            np.testing.assert_array_equal(_frame(ctx, exact, tf, 128, 160), _frame(ctx, learned, tf, 128, 160))
+        ls = vol.learned_stats()
+        assert ls["cells"] > 0 and ls["learned_transparent"] > 0
+    finally:
+        for v in views:
+            v.free()
+        vol.set_mlp(None)
+        mlp.free()
+        for t in tfs:
+            t.free()
+        vol.free()
+
+
 def test_learned_skip_gain_over_no_skipping(ctx):
     """The trained predictor against the method without it: the same frames
     (within 1/255) from far fewer executed samples and less time."""

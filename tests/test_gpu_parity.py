@@ -353,6 +353,43 @@ def test_skip_lossless_at_axis_views(ctx, dtype):
     v.free()
 
 
+@pytest.mark.parametrize("dtype", ["u8", "f32"])
+def test_macrocell_edges_lossless(ctx, dtype):
+    """Every macrocell edge (ivr_volume_set_macrocell: 4, 8, 16, 32 voxels)
+    renders the unskipped frame bit for bit, through a view set before the
+    switch (its frame is derived again on the next render); 8-voxel cells
+    execute fewer samples than 16-voxel ones; other edges are rejected and
+    leave the volume as it was."""
+    vol = synth.blob_volume((72, 64, 56), n_blobs=10, seed=13, dtype=dtype, zero_fraction=0.6, cell=8)
+    v = ctx.load_volume(vol).bricks(2, 2, 1)
+    assert v.macrocell_edge() == 16
+    tf = ctx.transfer_function().set_lut(synth.ramp_tf(256), 0, 1.0, api.TF_F2B)
+    st = orbit_state(35, 25, 64, 64, fovy=30.0, alpha=1.0)
+    plain = ctx.view().set(v, st, api.config_params(skip=False))
+    ref, _ = dev_frame(64, 64)
+    plain.render(tf, ref.data_ptr())
+    ref = host(ref)
+    n_plain = plain.census(tf)["executed"]
+    plain.free()
+    view = ctx.view().set(v, st, api.config_params())
+    execd = {}
+    for cell in (16, 8, 4, 32):
+        v.macrocell(cell)
+        assert v.macrocell_edge() == cell
+        o32, _ = dev_frame(64, 64)
+        view.render(tf, o32.data_ptr())
+        assert np.array_equal(bits(host(o32)), bits(ref)), cell
+        execd[cell] = view.census(tf)["executed"]
+        assert execd[cell] < n_plain, cell
+    assert execd[8] < execd[16], execd
+    for bad in (0, 3, 12, 64):
+        with pytest.raises(Exception):
+            v.macrocell(bad)
+    assert v.macrocell_edge() == 32
+    view.free()
+    v.free()
+
+
 def test_tiles_equal_full_frame(ctx):
     vol = make_config_volume((40, 40, 40), "u8", 9)
     st = orbit_state(60, -20, 80, 64, fovy=30.0, alpha=1.0)
