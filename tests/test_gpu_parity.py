@@ -390,6 +390,32 @@ def test_macrocell_edges_lossless(ctx, dtype):
     v.free()
 
 
+def test_view_follows_brick_rebuilds(ctx):
+    """A view set before the volume's bricks are rebuilt (another brick
+    grid, corner-packed copies off) renders what a view set afterwards
+    renders, bit for bit: its frame is derived again, never from the freed
+    bricks."""
+    vol = make_config_volume((48, 40, 44), "u16", 21)
+    v = ctx.load_volume(vol).bricks(2, 2, 1)
+    tf = ctx.transfer_function().set_lut(synth.ramp_tf(256), 0, 256.0 / 65536.0, api.TF_F2B)
+    st = orbit_state(120, 30, 56, 48, fovy=30.0, alpha=1.0)
+    old = ctx.view().set(v, st, api.config_params())
+    o32, _ = dev_frame(48, 56)
+    old.render(tf, o32.data_ptr())
+    for change in (lambda: v.bricks(1, 2, 3), lambda: v.quads(False), lambda: v.bricks(1, 1, 1)):
+        change()
+        fresh = ctx.view().set(v, st, api.config_params())
+        a, _ = dev_frame(48, 56)
+        b, _ = dev_frame(48, 56)
+        old.render(tf, a.data_ptr())
+        fresh.render(tf, b.data_ptr())
+        assert np.array_equal(bits(host(a)), bits(host(b)))
+        assert old.info()["nbricks"] == fresh.info()["nbricks"]
+        fresh.free()
+    old.free()
+    v.free()
+
+
 def test_tiles_equal_full_frame(ctx):
     vol = make_config_volume((40, 40, 40), "u8", 9)
     st = orbit_state(60, -20, 80, 64, fovy=30.0, alpha=1.0)
