@@ -437,15 +437,17 @@ __device__ __forceinline__ int cfg_first_ge(float t0, float dt, float idt, float
 
 
 // One brick of the CONFIG march: samples tin_k <= t_i < tout_k of the ray's
-// lattice, front-to-back into acc.  One loop iteration is one lattice index
-// for every lane, so the lanes of a warp stay in step.  With a macrocell grid
-// a lane checks the cell of its sample (by the same index arithmetic the
-// sampler uses) only when it passes the exit of the last opaque cell it
-// checked: a transparent cell's samples are stepped over up to two samples
-// before the ray leaves the cell's box (each skipped sample lies in the cell,
-// so it would have had zero opacity and left acc unchanged); an opaque cell's
-// samples are taken up to one past the exit without further checks.  Every
-// sample that is taken is computed exactly as without skipping.
+// lattice, front-to-back into acc.  One loop iteration takes one lattice
+// index (two with PAIR) for every lane, so the lanes of a warp stay in step.
+// With a macrocell grid a lane checks the cell of its sample (by the same
+// index arithmetic the sampler uses) only when it passes the exit of the last
+// opaque cell it checked.  A transparent cube's samples are stepped over to
+// just past its exit (or to two samples before it, where rounding at a face
+// leaves the last one in doubt), and successive cubes are leapt within the
+// same iteration; each skipped sample lies in a transparent cell, so it would
+// have had zero opacity and left acc unchanged.  An opaque cell's samples are
+// taken up to one past its exit without further checks.  Every sample that is
+// taken is computed exactly as without skipping.
 template <int DT, bool SKIP, bool CENSUS, bool PAIR>
 __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *empty, float dx, float dy, float dz,
                           float idx, float idy, float idz, float t0, float dt, float idt, float4 &acc, bool &done,
