@@ -75,3 +75,6 @@ def test_errors_without_device(gpu_lib):
     assert gpu_lib.ivr_destroy(None) == -1
     assert gpu_lib.ivr_create(0, 0, None) == -1
     assert gpu_lib.ivr_last_error(None) == b"null context"
+    assert gpu_lib.ivr_volume_set_macrocell(None, 8) == -1
+    assert gpu_lib.ivr_volume_macrocell(None, None) == -1
+    assert gpu_lib.ivr_volume_set_quads(None, 1) == -1
