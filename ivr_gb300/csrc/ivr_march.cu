@@ -478,7 +478,7 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
             // the sample's macrocell: its voxel cell (the sampler's own index
             // arithmetic) over the macrocell edge (cells are never negative:
             // the sampler clamps them)
-            const int cs = b.cshift;
+            const int cs = b.cshift, edge = 1 << cs;
             const int cj = c0.j >> cs, ci = c0.i >> cs, ck = c0.k >> cs;
             // r >= 1: the cube of cells within r-1 of this one is transparent
             const int r = empty[(ck * b.mcy + ci) * b.mcx + cj];
@@ -486,9 +486,9 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
             // the voxel plane of the face through which the ray leaves that
             // cube (or this one opaque cell), per axis, and the lattice index
             // of the exit; approximate, the margins absorb its rounding
-            const float fx = (float) ((L.sx > 0.0f ? cj + rr : cj - rr + 1) << cs);
-            const float fy = (float) ((L.sy > 0.0f ? ci + rr : ci - rr + 1) << cs);
-            const float fz = (float) ((L.sz > 0.0f ? ck + rr : ck - rr + 1) << cs);
+            const float fx = (float) ((L.sx > 0.0f ? cj + rr : cj - rr + 1) * edge);
+            const float fy = (float) ((L.sy > 0.0f ? ci + rr : ci - rr + 1) * edge);
+            const float fz = (float) ((L.sz > 0.0f ? ck + rr : ck - rr + 1) * edge);
             const float qx = L.sx != 0.0f ? (fx - L.bx) * isx : FLT_MAX;
             const float qy = L.sy != 0.0f ? (fy - L.by) * isy : FLT_MAX;
             const float qz = L.sz != 0.0f ? (fz - L.bz) * isz : FLT_MAX;
