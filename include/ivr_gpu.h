@@ -50,7 +50,7 @@ extern "C" {
 #define IVR_ERR_CUDA (-2)        /* a CUDA call failed */
 #define IVR_ERR_NOMEM (-3)       /* allocation refused by the HBM budget or by CUDA */
 #define IVR_ERR_IO (-4)          /* volume file missing or short */
-#define IVR_ERR_UNSUPPORTED (-5) /* valid request this build does not serve */
+#define IVR_ERR_UNSUPPORTED (-5) /* a valid request the library does not serve */
 #define IVR_ERR_TIMEOUT (-6)     /* a bounded device wait gave up */
 
 typedef struct ivr_ctx ivr_ctx;
