@@ -145,7 +145,7 @@ void finish_slot(ivr_server *s, Slot &sl)
 {
     const double t = now_s();
     float ms = 0.0f;
-    if (cudaEventElapsedTime(&ms, sl.t0, sl.t1) == cudaSuccess) s->gpu_s += ms / 1000.0;
+    const double batch_s = cudaEventElapsedTime(&ms, sl.t0, sl.t1) == cudaSuccess ? ms / 1000.0 : 0.0;
     for (size_t i = 0; i < sl.reqs.size(); i++) {
         Req &q = sl.reqs[i];
         if (!q.direct) memcpy(q.r.rgba8_host, (char *) sl.pinned + sl.offs[i], q.bytes);
@@ -155,6 +155,7 @@ void finish_slot(ivr_server *s, Slot &sl)
     sl.offs.clear();
     std::lock_guard<std::mutex> lock(s->mu);
     sl.busy = false;
+    s->gpu_s += batch_s;  // read under the same lock by ivr_server_times
     s->finish_s += now_s() - t;
 }
 
