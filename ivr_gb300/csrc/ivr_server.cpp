@@ -50,6 +50,8 @@ double now_s()
 
 struct Req {
     ivr_request r;
+    ivr_volume *vol;  // r.volume's handle and dtype, resolved under the lock at submit
+    int dtype;
     double t_submit;
     int vw, vh;
     size_t bytes;
@@ -110,6 +112,7 @@ struct ivr_server {
     int listen_fd = -1;
     std::thread acceptor;
     std::vector<std::thread> conns;
+    std::vector<int> conn_fds;  // open client sockets (under mu), shut down by ivr_server_destroy
     std::atomic<bool> net_stop{false};
     int net_tf = 0;
     int net_volume = 0;
@@ -205,7 +208,7 @@ bool dispatch(ivr_server *s, Slot &sl)
     {
         std::lock_guard<std::mutex> lock(s->mu);
         if (s->queue.empty()) return false;
-        const int dtype = s->vol_dtype[s->queue.front().r.volume];
+        const int dtype = s->queue.front().dtype;
         size_t used = 0;
         for (auto it = s->queue.begin(); it != s->queue.end() && (int) take.size() < s->cfg.max_batch_frames;) {
             if (it->bytes > s->cfg.arena_bytes) {  // larger than an arena: never admitted
@@ -213,7 +216,7 @@ bool dispatch(ivr_server *s, Slot &sl)
                 it = s->queue.erase(it);
                 continue;
             }
-            if (s->vol_dtype[it->r.volume] != dtype) {
+            if (it->dtype != dtype) {
                 ++it;
                 continue;
             }
@@ -225,7 +228,7 @@ bool dispatch(ivr_server *s, Slot &sl)
     }
     for (auto &q : never) complete(s, q, IVR_ERR_NOMEM, 0.0);
     if (take.empty()) return !never.empty();
-    const int dtype = s->vol_dtype[take[0].r.volume];
+    const int dtype = take[0].dtype;
     ivr_batch *&b = sl.batch[dtype];
     if (!b) {
         if (ivr_batch_create(s->ctx, s->cfg.max_batch_frames, &b) != IVR_OK) b = nullptr;
@@ -245,7 +248,7 @@ bool dispatch(ivr_server *s, Slot &sl)
         ivr_tf *tf = (q.r.tf >= 0 && q.r.tf < (int) s->tfs.size()) ? s->tfs[q.r.tf] : nullptr;
         int rc = b ? IVR_OK : IVR_ERR_NOMEM;
         if (rc == IVR_OK && !tf) rc = IVR_ERR_INVALID;
-        if (rc == IVR_OK) rc = ivr_set_view(view, s->vols[q.r.volume], &q.r.state, &s->params);
+        if (rc == IVR_OK) rc = ivr_set_view(view, q.vol, &q.r.state, &s->params);
         if (rc == IVR_OK) rc = ivr_batch_add(b, view, tf, nullptr, (uint8_t *) sl.arena + off);
         if (rc != IVR_OK) {
             complete(s, q, rc, sl.t_start);
@@ -356,8 +359,7 @@ bool page_locked(const void *p, size_t n)
 
 int submit_req(ivr_server *s, const ivr_request *r, std::shared_ptr<std::promise<int>> notify)
 {
-    if (r->volume < 0 || r->volume >= (int) s->vols.size()) return IVR_ERR_INVALID;
-    if (!r->rgba8_host) return IVR_ERR_INVALID;
+    if (r->volume < 0 || !r->rgba8_host) return IVR_ERR_INVALID;
     Req q;
     q.r = *r;
     q.t_submit = now_s();
@@ -370,7 +372,9 @@ int submit_req(ivr_server *s, const ivr_request *r, std::shared_ptr<std::promise
     memset(&q.c, 0, sizeof(q.c));
     {
         std::lock_guard<std::mutex> lock(s->mu);
-        if (s->stop) return IVR_ERR_INVALID;
+        if (s->stop || r->volume >= (int) s->vols.size()) return IVR_ERR_INVALID;
+        q.vol = s->vols[r->volume];
+        q.dtype = s->vol_dtype[r->volume];
         s->queue.push_back(q);
     }
     s->cv_work.notify_one();
@@ -430,6 +434,16 @@ void serve_conn(ivr_server *s, int fd)
         if (fut.get() != IVR_OK) break;
         if (!send_all(fd, frame.data(), frame.size())) break;
     }
+    {
+        // untracked first, so that ivr_server_destroy never shuts down a
+        // descriptor number that has been reused
+        std::lock_guard<std::mutex> lock(s->mu);
+        for (size_t i = 0; i < s->conn_fds.size(); i++)
+            if (s->conn_fds[i] == fd) {
+                s->conn_fds.erase(s->conn_fds.begin() + (long) i);
+                break;
+            }
+    }
     close(fd);
 }
 
@@ -442,6 +456,7 @@ void accept_loop(ivr_server *s)
             continue;
         }
         std::lock_guard<std::mutex> lock(s->mu);
+        s->conn_fds.push_back(fd);
         s->conns.emplace_back(serve_conn, s, fd);
     }
 }
@@ -581,7 +596,11 @@ int ivr_server_times(ivr_server *s, double *gpu_s, double *dispatch_s, double *f
 
 int ivr_server_listen(ivr_server *s, int port, int volume, int tf, int *bound_port)
 {
-    if (!s || s->listen_fd >= 0 || volume < 0 || volume >= (int) s->vols.size()) return IVR_ERR_INVALID;
+    if (!s || s->listen_fd >= 0 || volume < 0) return IVR_ERR_INVALID;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        if (volume >= (int) s->vols.size()) return IVR_ERR_INVALID;
+    }
     int fd = socket(AF_INET, SOCK_STREAM, 0);
     if (fd < 0) return IVR_ERR_IO;
     int one = 1;
@@ -628,7 +647,10 @@ int ivr_server_destroy(ivr_server *s)
     if (s->copier.joinable()) s->copier.join();
     std::vector<std::thread> conns;
     {
+        // the queue is drained: wake connections waiting for a client's next
+        // STATE, so that they end
         std::lock_guard<std::mutex> lock(s->mu);
+        for (int fd : s->conn_fds) shutdown(fd, SHUT_RDWR);
         conns.swap(s->conns);
     }
     for (auto &t : conns)

@@ -125,7 +125,16 @@ def test_tcp_front_end(vols):
         fin = orbit_state(0, 0, 8, 8)
         fin.finish = 1
         s.sendall(state_bytes(fin))
+    # a client that stays connected without sending: closing the server
+    # shuts its connection down instead of waiting for it
+    idle = socket.create_connection(("127.0.0.1", port))
+    idle.settimeout(30)
     srv.close()
+    try:
+        assert idle.recv(1) == b""
+    except ConnectionResetError:
+        pass
+    idle.close()
     for st, data in frames:
         assert len(data) == 64 * 48 * 4
         img = np.frombuffer(data, np.uint8).reshape(48, 64, 4)
