@@ -740,10 +740,10 @@ int ivr_volume_load_file(ivr_ctx *c, const char *path, int w, int h, int d, int 
         return fail(c, IVR_ERR_INVALID, "bad volume shape or dtype");
     if ((long long) w * h * d >= (1LL << 32)) return fail(c, IVR_ERR_UNSUPPORTED, "volume of 2^32 or more voxels");
     const size_t bytes = (size_t) w * h * d * dtype_size(dtype);
+    CK(c, cudaSetDevice(c->device));
     FILE *fp = fopen(path, "rb");
     if (!fp) return fail(c, IVR_ERR_IO, "cannot open %s", path);
     setvbuf(fp, nullptr, _IONBF, 0);  // chunks go straight into the staging buffers
-    CK(c, cudaSetDevice(c->device));
     ivr_volume *v = new ivr_volume();
     v->ctx = c;
     v->w = w; v->h = h; v->d = d; v->dtype = dtype;
