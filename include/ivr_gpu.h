@@ -33,6 +33,10 @@
  * thread-safe: use one context per host thread, or serialise calls.  A view
  * owns the work counter of its launches: launches of one view must be
  * ordered (one stream); use one view per stream for concurrent frames.
+ * ivr_create, ivr_destroy, ivr_device_alloc, ivr_host_alloc, the volume
+ * loads, ivr_volume_gradient and ivr_volume_set_macrocell make the
+ * context's device current (cudaSetDevice) and leave it current; the other
+ * calls work on the current device, which must be the context's.
  * Images are [h][w] rows of RGBA, row 0 at the bottom (GL raster order).
  */
 #ifndef IVR_GPU_H
@@ -195,19 +199,22 @@ int ivr_volume_minmax(ivr_volume *vol, float *mn, float *mx);
 int ivr_volume_histogram(ivr_volume *vol, int *hist, int hsize);
 /* The same min, max and histogram without allocating any device memory.
  * This entry point has no counterpart in the reference.  It is for callers
- * that must not call cudaMalloc/cudaFree here: a steering server whose HBM
- * budget is fully given to resident volumes, a frame loop that cannot take
- * the device-wide synchronisation cudaFree implies while other streams are
- * rendering, or code that runs while a stream is being captured.  Its
- * scratch is one static device array (about 261 KiB) that every GPU loading
- * this library holds until the process exits, so hsize is limited to
- * 65536 bins (IVR_ERR_INVALID above that).  The first call on a device looks
- * up that array's address (and loads the library's kernels there if they
- * are not loaded yet): make it before any stream capture.  Calls share the
- * array and it keeps the last call's contents (the bins are cleared at the
- * start of each call): calls that overlap on the GPU -- on two streams or
- * from two threads -- race.  Outputs are host memory; the call waits for
- * them on `stream`. */
+ * that cannot call cudaMalloc/cudaFree where they compute a LUT: a steering
+ * server whose HBM budget is fully given to resident volumes (an allocation
+ * there fails or evicts a volume), and a frame loop that renders on other
+ * streams meanwhile (cudaFree waits for the whole device, stalling them).
+ * Its scratch is one static device array (about 261 KiB) that every GPU
+ * loading this library holds until the process exits, so hsize is limited
+ * to 65536 bins (IVR_ERR_INVALID above that).  The first call on a device
+ * looks up that array's address with cudaGetSymbolAddress (and loads the
+ * library's kernels there if they are not loaded yet); make that first call
+ * before any stream capture.  Calls share the array and it keeps the last
+ * call's contents (the bins are cleared at the start of each call): calls
+ * that overlap on the GPU -- on two streams or from two threads -- race.
+ * The work is queued on `stream`; the call then copies the results into the
+ * caller's host arrays and waits for `stream` before it returns.  The
+ * volume's device is current during the call; the caller's current device
+ * is restored before it returns. */
 int ivr_volume_histogram_noalloc(ivr_volume *vol, int *hist, int hsize, float *mn, float *mx, void *stream);
 
 /* --- transfer function (initcolormap, initvolluts, inittransferfunc) ---- */

@@ -877,10 +877,17 @@ int ivr_volume_histogram_noalloc(ivr_volume *v, int *hist, int hsize, float *mn,
     if (hsize < 1 || hsize > kNoAllocMaxBins)
         return fail(c, IVR_ERR_INVALID, "hsize %d is outside [1, %d], the bins the allocation-free histogram holds",
                     hsize, kNoAllocMaxBins);
+    // the volume's device is made current for the call and the caller's
+    // current device is put back afterwards, whatever the outcome
+    int prev = -1;
+    CK(c, cudaGetDevice(&prev));
     CK(c, cudaSetDevice(c->device));
     float mm[2];
-    CK(c, noalloc_histogram(v->d_full, v->dtype, (long long) v->w * v->h * v->d, hsize, hist, mm,
-                            (cudaStream_t) stream));
+    cudaError_t e = noalloc_histogram(v->d_full, v->dtype, (long long) v->w * v->h * v->d, hsize, hist, mm,
+                                      (cudaStream_t) stream);
+    cudaError_t r = cudaSetDevice(prev);
+    CK(c, e);
+    CK(c, r);
     *mn = mm[0];
     *mx = mm[1];
     return IVR_OK;

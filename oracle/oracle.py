@@ -19,7 +19,9 @@ from ivr_gb300.state import IvrState
 HERE = os.path.dirname(os.path.abspath(__file__))
 O2_PATH = os.path.join(HERE, "liboracle.so")
 O1_PATH = os.path.join(HERE, "_ref", "libivr_ref.so")
-REF_SRC = "/root/reference"
+# where the reference checkout lies: IVR_REFERENCE_SRC, else the checkout this
+# build was set up with
+REF_SRC = os.environ.get("IVR_REFERENCE_SRC") or "/root/reference"
 
 U8, U16, F32 = 0, 1, 2
 PRESET_REF, PRESET_CONFIG = 0, 1
@@ -222,6 +224,19 @@ def lut_for(vol: np.ndarray, cm: int):
     hsize = o2().orc_minmax(v.ctypes.data, DT_CODE[v.dtype], v.size, ctypes.byref(mn), ctypes.byref(mx))
     lut = colormap(cm, hsize, mn.value, mx.value)
     return lut, int(mn.value + 0.5)
+
+
+def minmax_histogram(vol: np.ndarray, hsize: int = 0):
+    """initvolluts' min, max and histogram (mathutil.c:444-470) over the
+    whole volume: (mn, mx, hist) with hsize bins (0: (int)(max-min+1))."""
+    v = np.ascontiguousarray(vol)
+    mn, mx = ctypes.c_float(), ctypes.c_float()
+    full = o2().orc_minmax(v.ctypes.data, DT_CODE[v.dtype], v.size, ctypes.byref(mn), ctypes.byref(mx))
+    n = hsize or full
+    hist = np.zeros(n, np.int32)
+    o2().orc_histogram(v.ctypes.data, DT_CODE[v.dtype], v.size, mn.value, n,
+                       hist.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return mn.value, mx.value, hist
 
 
 def quantize(x: np.ndarray) -> np.ndarray:

@@ -79,3 +79,21 @@ def test_reference_arm_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
     assert "layout" not in line["config"]
+
+
+def test_reference_arm_learned_line_has_our_config():
+    """The reference arm on the learned-skip workload (the small variant):
+    the oracle on bands of the same frames, and the same config dict as the
+    GPU arm's line, so that the two lines describe one workload."""
+    import argparse
+    import json
+    import bench
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
+                        "learned_256", "--steps", "2", "--warmup", "1"], env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["dtype"] == "u16"
+    args = argparse.Namespace(gpus=1)
+    assert line["config"] == bench.learned_config(args, bench.LEARNED_SMALL)
