@@ -52,7 +52,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 from ivr_gb300 import workloads  # noqa: E402
-from ivr_gb300.workloads import BATCH, LEARNED, LEARNED_SMALL, RENDER, SERVE  # noqa: E402
+from ivr_gb300.workloads import BATCH, LEARNED, LEARNED_CASES, LEARNED_SMALL, RENDER, SERVE  # noqa: E402
 
 METRIC = "frames/s & Gsamples/s, learned-skip vs plain GPU at <=1/255 err; p99 ms"
 PROFILES = os.path.join(ROOT, "profiles")
@@ -162,6 +162,28 @@ def _gen_device():
         return None
 
 
+class nvtx_range:
+    """An NVTX range around a timed region (for ncu --nvtx-include);
+    nothing when NVTX is unavailable."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __enter__(self):
+        try:
+            import torch
+            torch.cuda.nvtx.range_push(self.name)
+            self.on = True
+        except Exception:
+            self.on = False
+        return self
+
+    def __exit__(self, *a):
+        if self.on:
+            import torch
+            torch.cuda.nvtx.range_pop()
+
+
 def band_parity(got32, got8, ref32, ref8, rows):
     """Largest differences of one band of a GPU frame against the oracle's."""
     r0, r1 = rows
@@ -215,14 +237,17 @@ def oracle_bands(vol, prep, frames, bricks, step, term, scale, threads, budget_s
 
 def learned_config(args, L):
     w, h = L["image"]
-    return {"workload": "learned_256" if L is LEARNED_SMALL else "learned_1024",
+    name = [k for k, c in LEARNED_CASES.items() if c is L][0]
+    return {"workload": name,
             "volume": "x".join(map(str, L["shape"])) + f" u16, one brick, {L['n_blobs']} blobs, "
                       f"{int(L['zero_fraction'] * 100)}% zero 16^3 macrocells",
             "image": f"{w}x{h}", "tfs": f"{L['tfs']} random 16-knot piecewise-linear TFs, 60% zero opacity knots",
             "lut": "256-entry RGBA FP32, index (int)(v*256/65536)",
             "step_voxels": L["step"], "early_termination_alpha": L["term"],
-            "skip": f"learned grid (26-64-64-1 BF16 MLP, trained on {L['train_tfs']} TFs), judged 1 tile in "
-                    f"{L['judge_stride']} at 1/255 with exact-grid fallback",
+            "skip": {"learned": f"learned grid (26-64-64-1 BF16 MLP, trained on {L['train_tfs']} TFs), judged 1 "
+                                f"tile in {L['judge_stride']} at 1/255 with exact-grid fallback",
+                     "grid": "exact macrocell grid of 16^3-voxel cells",
+                     "none": "none (every lattice point)"}[getattr(args, "skip", "learned")],
             "step": "one frame: a new view under the next TF",
             "l2": "inputs larger than L2 (2 GiB volume resident)", "parallelism": f"replicas x{args.gpus}"}
 
@@ -261,7 +286,9 @@ def _learned_setup(ctx, L, vol, args):
     losses = mlp.train(L["epochs"], batch_rows=L["batch_rows"], lr=L["lr"], wneg=L["wneg"])
     t_train = time.perf_counter() - t0
     margin, recall = mlp.calibrate(L["slack"])
-    v.set_mlp(mlp, margin, certify=True)
+    v.set_mlp(mlp, margin, certify=not args.no_certify)
+    if args.linear or args.cell != 16:
+        v.quads(not args.linear).macrocell(args.cell)
     training = {"samples": n, "epochs": L["epochs"], "batch_rows": L["batch_rows"],
                 "loss_first": float(losses[0]), "loss_last": float(losses[-1]), "features_s": t_feat,
                 "train_s": t_train, "margin": margin, "recall_of_transparent_cells": recall}
@@ -344,7 +371,7 @@ def run_learned(args, quiet=False):
     import torch
     import torch.distributed as dist
     from ivr_gb300 import api
-    L = LEARNED_SMALL if args.workload == "learned_256" else LEARNED
+    L = LEARNED_CASES[args.workload]
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -362,10 +389,12 @@ def run_learned(args, quiet=False):
     # the method comparison renders every TF once with each method (so each
     # TF's grids are resident before the timed region) on views of its own
     states = workloads.learned_views(L, n=max(ntf, args.steps + args.warmup), seed_offset=77 + 7919 * rank)
-    methods = _methods(ctx, v, tfs, states, L, args, stream, local)
+    methods = None if args.no_methods else _methods(ctx, v, tfs, states, L, args, stream, local)
 
-    params = api.config_params(step=L["step"], term_alpha=L["term"], skip=api.SKIP_LEARNED,
-                               judge_stride=args.judge_stride or L["judge_stride"])
+    skip = {"learned": api.SKIP_LEARNED, "grid": api.SKIP_GRID, "none": api.SKIP_NONE}[args.skip]
+    params = api.config_params(step=L["step"], term_alpha=L["term"], skip=skip,
+                               judge_stride=args.judge_stride or L["judge_stride"],
+                               tiles=api.TILES_RASTER if args.tiles == "raster" else api.TILES_COST)
     view = ctx.view()
     o8 = torch.empty((h, w, 4), dtype=torch.uint8, device="cuda")
     nsteps = args.steps + args.warmup
@@ -377,6 +406,10 @@ def run_learned(args, quiet=False):
         view.render(tfs[t], None, o8.data_ptr(), sp)
 
     with torch.cuda.stream(stream):
+        if methods is None:  # every TF's grids built before the timed region, as the comparison does
+            for t in sorted({t for _, t in frames}):
+                view.set(v, frames[0][0], params)
+                view.render(tfs[t], None, o8.data_ptr(), sp)
         for k in range(args.warmup):
             frame(k)
         torch.cuda.synchronize()
@@ -385,7 +418,7 @@ def run_learned(args, quiet=False):
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
-        with ClockSampler(local) as clk:
+        with ClockSampler(local) as clk, nvtx_range("timed"):
             start.record(stream)
             for k in range(args.steps):
                 ev[k][0].record(stream)
@@ -461,7 +494,8 @@ def run_learned(args, quiet=False):
             "judge_timed_frames": judge_timed,
             "methods": methods,
             "training": training, "ingest": ingest,
-            "gpu_launches": args.steps * LAUNCHES_LEARNED,
+            "gpu_launches": args.steps * (LAUNCHES_LEARNED if skip == api.SKIP_LEARNED else
+                                          LAUNCHES_GRID if skip == api.SKIP_GRID else 1),
             "clocks": clk.summary(),
         }
         if not args.no_cpu_baseline and world == 1:
@@ -525,7 +559,7 @@ def run_reference_learned(args):
     if rank != 0:
         return
     from oracle import oracle
-    L = LEARNED_SMALL if args.workload == "learned_256" else LEARNED
+    L = LEARNED_CASES[args.workload]
     vol = workloads.learned_volume(L, device=_gen_device())
     luts = workloads.learned_tfs(L)
     nsteps = args.steps + args.warmup
@@ -680,7 +714,7 @@ def run_sorted(args, quiet=False, name="sorted_brick_512"):
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
-        with ClockSampler(local) as clk:
+        with ClockSampler(local) as clk, nvtx_range("timed"):
             start.record(stream)
             for k in range(args.steps):
                 ev[k][0].record(stream)
@@ -1079,7 +1113,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="learned_1024",
-                    choices=["learned_1024", "learned_256", "batch_64x4", "serve_32"] + sorted(RENDER))
+                    choices=sorted(LEARNED_CASES) + ["batch_64x4", "serve_32"] + sorted(RENDER))
+    ap.add_argument("--skip", default="learned", choices=["learned", "grid", "none"],
+                    help="learned workloads: the skipping of the timed frames (learned grid by default)")
+    ap.add_argument("--no-certify", action="store_true",
+                    help="learned workloads: learned grids without the cell-by-cell check against the exact test "
+                         "(the per-frame judge alone guards the frames)")
+    ap.add_argument("--no-methods", action="store_true",
+                    help="learned workloads: leave out the comparison of the three methods over every TF")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--serve-slots", type=int, default=0)
@@ -1100,7 +1141,7 @@ def main():
         return run_batch(args)
     if args.workload == "serve_32":
         return run_serve(args, sweep=[] if args.no_extras else [2.0, 3.0])
-    learned = args.workload in ("learned_1024", "learned_256")
+    learned = args.workload in LEARNED_CASES
     if args.impl == "reference":
         return run_reference_learned(args) if learned else run_reference_sorted(args, args.workload)
     if not learned:

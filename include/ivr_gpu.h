@@ -445,6 +445,14 @@ int ivr_composite(ivr_ctx *ctx, float *tilebuf_dev, const float *rcolorbuf_dev, 
 /* (uint8)(clamp(v,0,1) * 255 + 0.5) per float (main.c:1404). */
 int ivr_quantize(ivr_ctx *ctx, const float *in_dev, uint8_t *out_dev, long long n, void *stream);
 
+/* --- host plumbing (no counterpart in the reference, whose buffers are all
+ * host memory) ------------------------------------------------------------
+ * For C callers that hold no CUDA headers: a copy of `bytes` between any
+ * two of host and device memory, queued on `stream`, and a wait for
+ * everything queued on `stream`. */
+int ivr_copy(ivr_ctx *ctx, void *dst, const void *src, size_t bytes, void *stream);
+int ivr_stream_wait(ivr_ctx *ctx, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -180,6 +180,8 @@ SIGNATURES = {
     "ivr_sample_peak_layout": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _P]),
     "ivr_composite": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "ivr_quantize": (_I, [_P, _P, _P, ctypes.c_longlong, _P]),
+    "ivr_copy": (_I, [_P, _P, _P, ctypes.c_size_t, _P]),
+    "ivr_stream_wait": (_I, [_P, _P]),
 }
 
 _lib = None

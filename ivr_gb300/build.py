@@ -17,6 +17,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libivr_gpu.so")
+# the reference's own names over LIB (include/ivr_compat.h)
+COMPAT_SRC = os.path.join(HERE, "compat", "ivr_compat.c")
+COMPAT_LIB = os.path.join(HERE, "libivr_compat.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 CUDA_INC = os.path.join(os.path.dirname(os.path.dirname(NVCC)), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -61,6 +64,11 @@ def build(verbose: bool = False) -> str:
     tmp = LIB + ".tmp"
     _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fPIC"], log)
     os.replace(tmp, LIB)
+    tmp = COMPAT_LIB + ".tmp"
+    _run(["gcc", "-std=gnu99", "-O2", "-fPIC", "-shared", "-Wall", "-Wextra", "-Wno-unused-parameter",
+          "-I" + os.path.join(ROOT, "include"), COMPAT_SRC, "-o", tmp, "-L" + HERE, "-l:libivr_gpu.so",
+          "-Wl,-rpath,$ORIGIN"], log)
+    os.replace(tmp, COMPAT_LIB)
     if verbose:
         for cmd, out in log:
             if out.strip():

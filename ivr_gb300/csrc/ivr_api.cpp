@@ -1518,4 +1518,20 @@ int ivr_quantize(ivr_ctx *c, const float *in, uint8_t *out, long long n, void *s
     return IVR_OK;
 }
 
+int ivr_copy(ivr_ctx *c, void *dst, const void *src, size_t bytes, void *stream)
+{
+    if (!c) return IVR_ERR_INVALID;
+    if (bytes > 0 && (!dst || !src)) return fail(c, IVR_ERR_INVALID, "null copy buffer");
+    if (bytes == 0) return IVR_OK;
+    CK(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, (cudaStream_t) stream));
+    return IVR_OK;
+}
+
+int ivr_stream_wait(ivr_ctx *c, void *stream)
+{
+    if (!c) return IVR_ERR_INVALID;
+    CK(c, cudaStreamSynchronize((cudaStream_t) stream));
+    return IVR_OK;
+}
+
 }  // extern "C"

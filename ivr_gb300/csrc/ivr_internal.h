@@ -11,7 +11,10 @@ namespace ivr {
 constexpr int kMaxBricks = IVR_MAX_BRICKS;
 constexpr int kCell = 16;  // default macrocell edge in voxels (ivr_volume_set_macrocell)
 constexpr int kMinCell = 4, kMaxCell = 32;  // the edges a volume may use: powers of two
-constexpr int kDistCap = 8;  // largest transparent radius stored per macrocell
+#ifndef IVR_DIST_CAP
+#define IVR_DIST_CAP 8
+#endif
+constexpr int kDistCap = IVR_DIST_CAP;  // largest transparent radius stored per macrocell
 
 // One brick as the march kernels see it.  Geometry follows the reference's
 // per-rank AABB (main.c:552-618): bmin and w/h/d from the brick's world

@@ -42,9 +42,14 @@ LEARNED = dict(shape=(1024, 1024, 1024), dtype="u16", n_blobs=256, sigma_scale=(
                zero_fraction=0.7, image=(1920, 1080), bricks=(1, 1, 1),
                step=0.5, term=0.99, fovy=30.0, seed=3, tfs=50, train_tfs=8, epochs=30, batch_rows=8192, lr=2e-3,
                wneg=4.0, slack=0.02, judge_stride=16, frames=3)
-# the same at 256^3 and 1280x720 with 10 TFs: the case ncu captures
+# the same at 256^3 and 1280x720 with 10 TFs: a small case for quick runs
 LEARNED_SMALL = dict(LEARNED, shape=(256, 256, 256), n_blobs=32, sigma_scale=(8 / 32) ** (1 / 3), image=(1280, 720),
                      tfs=10, train_tfs=4, epochs=5)
+# the learned_1024 volume at half the resolution (the same blobs, 32^3
+# macrocells, 256 MiB + 1 GiB of corner-packed copy), the same image and
+# TFs: the case ncu captures in full
+LEARNED_HALF = dict(LEARNED, shape=(512, 512, 512))
+LEARNED_CASES = {"learned_1024": LEARNED, "learned_256": LEARNED_SMALL, "learned_512": LEARNED_HALF}
 
 BATCH = dict(base="sorted_brick_512", views=64, tfs=4, sizes=[(256, 256), (512, 512), (1024, 1024), (1920, 1080)],
              steps=(0.25, 1.0), seed=40)
