@@ -184,6 +184,70 @@ class nvtx_range:
             torch.cuda.nvtx.range_pop()
 
 
+class InFlight:
+    """Frames in flight: frame k renders with view k % S on stream k % S, so
+    that frame k+1's tiles fill the SMs that frame k's tail leaves idle.  Each
+    view and stream has its own RGBA8 frame in device memory and one in
+    page-locked host memory (which its launches store into directly)."""
+
+    def __init__(self, ctx, S, stream, h, w):
+        import torch
+        self.S = max(1, S)
+        self.views = [ctx.view() for _ in range(self.S)]
+        self.streams = [stream] + [torch.cuda.Stream() for _ in range(self.S - 1)]
+        self.dev = [torch.empty((h, w, 4), dtype=torch.uint8, device="cuda") for _ in range(self.S)]
+        self.host = [torch.empty((h, w, 4), dtype=torch.uint8).pin_memory() for _ in range(self.S)]
+
+    def render(self, k, vol, state, params, tf, host=False):
+        q = k % self.S
+        self.views[q].set(vol, state, params)
+        self.views[q].render(tf, None, (self.host if host else self.dev)[q].data_ptr(), self.streams[q].cuda_stream)
+
+    def timed(self, ks, run, ev=None):
+        """run(k) for k in ks between events on the first stream, which the
+        other streams wait on and join: device milliseconds."""
+        import torch
+        first = self.streams[0]
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(first)
+        for q in self.streams[1:]:
+            q.wait_event(start)
+        for n, k in enumerate(ks):
+            q = self.streams[k % self.S]
+            if ev:
+                ev[n][0].record(q)
+            run(k)
+            if ev:
+                ev[n][1].record(q)
+        for q in self.streams[1:]:
+            e = torch.cuda.Event()
+            e.record(q)
+            first.wait_event(e)
+        stop.record(first)
+        torch.cuda.synchronize()
+        return start.elapsed_time(stop)
+
+    def wall(self, ks, run):
+        """run(k) for k in ks, host seconds until every stream is done."""
+        import torch
+        t0 = time.perf_counter()
+        for k in ks:
+            run(k)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    def judge_stats(self):
+        tot = {}
+        for vw in self.views:
+            for key, val in vw.judge_stats().items():
+                tot[key] = max(tot.get(key, 0), val) if key == "worst" else tot.get(key, 0) + val
+        return tot
+
+    def free(self):
+        for vw in self.views:
+            vw.free()
+
+
 def band_parity(got32, got8, ref32, ref8, rows):
     """Largest differences of one band of a GPU frame against the oracle's."""
     r0, r1 = rows
@@ -249,6 +313,7 @@ def learned_config(args, L):
                      "grid": "exact macrocell grid of 16^3-voxel cells",
                      "none": "none (every lattice point)"}[getattr(args, "skip", "learned")],
             "step": "one frame: a new view under the next TF",
+            "frames_in_flight": getattr(args, "inflight", 3),
             "l2": "inputs larger than L2 (2 GiB volume resident)", "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -395,60 +460,60 @@ def run_learned(args, quiet=False):
     params = api.config_params(step=L["step"], term_alpha=L["term"], skip=skip,
                                judge_stride=args.judge_stride or L["judge_stride"],
                                tiles=api.TILES_RASTER if args.tiles == "raster" else api.TILES_COST)
-    view = ctx.view()
-    o8 = torch.empty((h, w, 4), dtype=torch.uint8, device="cuda")
+    fl = InFlight(ctx, args.inflight, stream, h, w)
+    S = fl.S
+    view = fl.views[0]
     nsteps = args.steps + args.warmup
     frames = [(states[k], k % ntf) for k in range(nsteps)]
 
-    def frame(k):
+    def frame(k, host=False):
         st, t = frames[k]
-        view.set(v, st, params)
-        view.render(tfs[t], None, o8.data_ptr(), sp)
+        fl.render(k, v, st, params, tfs[t], host)
 
+    timed_ks = range(args.warmup, nsteps)
     with torch.cuda.stream(stream):
         if methods is None:  # every TF's grids built before the timed region, as the comparison does
             for t in sorted({t for _, t in frames}):
                 view.set(v, frames[0][0], params)
-                view.render(tfs[t], None, o8.data_ptr(), sp)
+                view.render(tfs[t], None, fl.dev[0].data_ptr(), sp)
         for k in range(args.warmup):
             frame(k)
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
         with ClockSampler(local) as clk, nvtx_range("timed"):
-            start.record(stream)
-            for k in range(args.steps):
-                ev[k][0].record(stream)
-                frame(args.warmup + k)
-                ev[k][1].record(stream)
-            stop.record(stream)
-            torch.cuda.synchronize()
+            t_ms = fl.timed(timed_ks, frame, ev)
         if world > 1:
             dist.barrier()
-        t_ms = start.elapsed_time(stop)
         frame_ms = [a.elapsed_time(b) for a, b in ev]
-        judge_timed = view.judge_stats()
+        judge_timed = fl.judge_stats()
 
-        # end to end through ivr_render_host: pinned host output, same frames
-        host8 = torch.empty((h, w, 4), dtype=torch.uint8).pin_memory().numpy()
+        # end to end: the same frames with the STATE from host memory and the
+        # RGBA8 frames stored into page-locked host memory by the launches
+        # themselves, S in flight, timed until the last frame is in host memory
+        for k in range(args.warmup):
+            frame(k, True)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        e2e_s = fl.wall(timed_ks, lambda k: frame(k, True))
+        # and one frame at a time through ivr_render_host (waits for each)
+        host8 = fl.host[0].numpy()
         e2e_view = ctx.view()
         for k in range(args.warmup):
             st, t = frames[k]
             e2e_view.render_host(v, tfs[t], st, params, host8, sp)
         torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
         t0 = time.perf_counter()
-        for k in range(args.steps):
-            st, t = frames[args.warmup + k]
+        for k in timed_ks:
+            st, t = frames[k]
             e2e_view.render_host(v, tfs[t], st, params, host8, sp)
-        e2e_s = time.perf_counter() - t0
+        sync_s = time.perf_counter() - t0
         e2e_view.free()
 
-    t_ms, e2e_ms = max_over_ranks([t_ms, e2e_s * 1000.0], "cuda")
+    t_ms, e2e_ms, sync_ms = max_over_ranks([t_ms, e2e_s * 1000.0, sync_s * 1000.0], "cuda")
     fps = whole_job_rate(args.steps, world, t_ms)
     e2e_fps = whole_job_rate(args.steps, world, e2e_ms)
     line = None
@@ -462,7 +527,7 @@ def run_learned(args, quiet=False):
             lattice += c["lattice"]
             executed += c["executed"]
             touched += c["touched_bytes"]
-        kavg = statistics.mean(frame_ms)
+        kavg = t_ms / args.steps  # device time per frame, frames overlapping
         peak, how = peaks()
         sample_peak = ctx.sample_peak(api.U16, sp)
         alg_bytes = touched / args.steps + w * h * 4
@@ -478,10 +543,15 @@ def run_learned(args, quiet=False):
             "gsamples_per_s": lattice / args.steps * fps / 1e9,
             "samples": {"lattice_per_frame": lattice / args.steps, "executed_per_frame": executed / args.steps,
                         "note": "lattice = plain method without skipping or termination"},
-            "frame_ms": {"mean": kavg, "p50": statistics.median(frame_ms), "max": max(frame_ms)},
+            "frame_ms": {"per_frame": kavg, "span_p50": statistics.median(frame_ms), "span_max": max(frame_ms),
+                         "note": f"per_frame = timed region / frames with {S} frames in flight; span = one "
+                                 f"frame's own start-to-end on its stream"},
             "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": 184,
                     "d2h_bytes_per_step": w * h * 4,
-                    "path": "ivr_render_host: host STATE in, RGBA8 to pinned host memory"},
+                    "path": f"ivr_set_view + ivr_render: host STATE in, each RGBA8 frame stored by its launch into "
+                            f"page-locked host memory, {S} frames in flight, timed until the last is in host memory",
+                    "one_at_a_time": {"value": whole_job_rate(args.steps, world, sync_ms), "unit": "frames/s",
+                                      "path": "ivr_render_host, which waits for each frame"}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": profiled_traffic(args.workload), "peak_source": how,
                          "algorithmic_bytes_per_launch": alg_bytes,
@@ -501,7 +571,7 @@ def run_learned(args, quiet=False):
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = _learned_cpu_baseline(ctx, v, vol, tfs, luts, frames[args.warmup:], L, params,
                                                          stream, args.cpu_budget)
-    view.free()
+    fl.free()
     v.set_mlp(None)
     mlp.free()
     for tf in tfs:
@@ -609,36 +679,29 @@ def sorted_config(args, wl, name):
             "step_voxels": wl["step"], "early_termination_alpha": wl["term"],
             "skip": f"macrocell grid of {args.cell}^3-voxel cells",
             "tile_order": "costliest first (estimated)" if args.tiles == "cost" else "row order",
+            "frames_in_flight": getattr(args, "inflight", 3),
             "tf": "256-entry RGBA FP32 ramp", "l2": "inputs larger than L2 (volume resident, > 129 MB)",
             "parallelism": f"replicas x{args.gpus}"}
 
 
-def measure_cells(v, view, tf, params, states, args, o8, stream, cell):
+def measure_cells(v, fl, view, tf, params, states, args, ref8, cell):
     """frames/s and executed samples of the timed views with the volume's
-    macrocell edge switched to `cell` (outside the headline's timed region),
-    and whether the last frame is the headline's frame bit for bit."""
+    macrocell edge switched to `cell` (outside the headline's timed region,
+    the same frames in flight), and whether the last frame is the headline's
+    frame bit for bit."""
     import torch
-    sp = stream.cuda_stream
-    ref = o8.clone()
     v.macrocell(cell)
-    with torch.cuda.stream(stream):
+    with torch.cuda.stream(fl.streams[0]):
         for k in range(args.warmup):
-            view.set(v, states[k], params)
-            view.render(tf, None, o8.data_ptr(), sp)
+            fl.render(k, v, states[k], params, tf)
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for k in range(args.steps):
-            view.set(v, states[args.warmup + k], params)
-            view.render(tf, None, o8.data_ptr(), sp)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    same = bool(torch.equal(o8, ref))
+        last = args.warmup + args.steps - 1
+        ms = fl.timed(range(args.warmup, last + 1), lambda k: fl.render(k, v, states[k], params, tf))
+    same = bool(torch.equal(fl.dev[last % fl.S], ref8))
     executed = 0
     for st in states[args.warmup:]:
         view.set(v, st, params)
-        executed += view.census(tf, sp)["executed"]
+        executed += view.census(tf, fl.streams[0].cuda_stream)["executed"]
     return {"fps": args.steps / (ms / 1000.0), "executed_per_frame": executed / args.steps,
             "last_frame_equal": same}
 
@@ -701,51 +764,48 @@ def run_sorted(args, quiet=False, name="sorted_brick_512"):
         touched += c["touched_bytes"]
     torch.cuda.synchronize()
 
-    def frame(k):
-        view.set(v, states[k], params)
-        view.render(tf, None, o8.data_ptr(), sp)
+    fl = InFlight(ctx, args.inflight, stream, h, w)
+    S = fl.S
 
+    def frame(k, host=False):
+        fl.render(k, v, states[k], params, tf, host)
+
+    timed_ks = range(args.warmup, args.warmup + args.steps)
     with torch.cuda.stream(stream):
         for k in range(args.warmup):
             frame(k)
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
         with ClockSampler(local) as clk, nvtx_range("timed"):
-            start.record(stream)
-            for k in range(args.steps):
-                ev[k][0].record(stream)
-                frame(args.warmup + k)
-                ev[k][1].record(stream)
-            stop.record(stream)
-            torch.cuda.synchronize()
+            t_ms = fl.timed(timed_ks, frame, ev)
         if world > 1:
             dist.barrier()
-        t_ms = start.elapsed_time(stop)
         kern_ms = [a.elapsed_time(b) for a, b in ev]
 
-        host8 = torch.empty((h, w, 4), dtype=torch.uint8).pin_memory().numpy()
         for k in range(args.warmup):
-            view.render_host(v, tf, states[k], params, host8, sp)
+            frame(k, True)
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
+        e2e_s = fl.wall(timed_ks, lambda k: frame(k, True))
+        host8 = fl.host[0].numpy()
         t0 = time.perf_counter()
-        for k in range(args.steps):
-            view.render_host(v, tf, states[args.warmup + k], params, host8, sp)
-        e2e_s = time.perf_counter() - t0
+        for k in timed_ks:
+            view.render_host(v, tf, states[k], params, host8, sp)
+        sync_s = time.perf_counter() - t0
+        o8.copy_(fl.dev[(args.warmup + args.steps - 1) % S])  # the last timed frame (other edges compare with it)
 
-    t_ms, e2e_ms = max_over_ranks([t_ms, e2e_s * 1000.0], "cuda")
+    t_ms, e2e_ms, sync_ms = max_over_ranks([t_ms, e2e_s * 1000.0, sync_s * 1000.0], "cuda")
     fps = whole_job_rate(args.steps, world, t_ms)
     e2e_fps = whole_job_rate(args.steps, world, e2e_ms)
     gsps = lattice * world / (t_ms / 1000.0) / 1e9
 
     line = None
     if rank == 0:
-        kavg = statistics.mean(kern_ms)
+        kavg = t_ms / args.steps  # device time per frame, frames overlapping
         peak, how = peaks()
         sample_peak = ctx.sample_peak(v.dtype, sp)
         layouts = {}
@@ -757,7 +817,7 @@ def run_sorted(args, quiet=False, name="sorted_brick_512"):
         other_cells = {}
         if world == 1 and not args.no_extras:
             for cell in ((8,) if args.cell != 8 else (16,)):
-                other_cells[f"{cell}^3"] = measure_cells(v, view, tf, params, states, args, o8, stream, cell)
+                other_cells[f"{cell}^3"] = measure_cells(v, fl, view, tf, params, states, args, o8, cell)
             v.macrocell(args.cell)
         alg_bytes = touched / args.steps + w * h * 4
         achieved = alg_bytes / (kavg / 1000.0) / 1e9
@@ -772,10 +832,15 @@ def run_sorted(args, quiet=False, name="sorted_brick_512"):
             "gsamples_per_s": gsps,
             "samples": {"lattice_per_frame": lattice / args.steps, "executed_per_frame": executed / args.steps,
                         "note": "lattice = plain method without skipping or termination"},
-            "kernel_ms": {"mean": kavg, "p50": statistics.median(kern_ms), "max": max(kern_ms)},
+            "frame_ms": {"per_frame": kavg, "span_p50": statistics.median(kern_ms), "span_max": max(kern_ms),
+                         "note": f"per_frame = timed region / frames with {S} frames in flight; span = one "
+                                 f"frame's own start-to-end on its stream"},
             "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": 184,
                     "d2h_bytes_per_step": w * h * 4,
-                    "path": "ivr_render_host: host STATE in, RGBA8 to pinned host memory"},
+                    "path": f"ivr_set_view + ivr_render: host STATE in, each RGBA8 frame stored by its launch into "
+                            f"page-locked host memory, {S} frames in flight, timed until the last is in host memory",
+                    "one_at_a_time": {"value": whole_job_rate(args.steps, world, sync_ms), "unit": "frames/s",
+                                      "path": "ivr_render_host, which waits for each frame"}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": profiled_traffic(name), "peak_source": how,
                          "algorithmic_bytes_per_launch": alg_bytes,
@@ -834,6 +899,7 @@ def run_sorted(args, quiet=False, name="sorted_brick_512"):
                                "sample": f"{one['bands']} bands, {one['seconds']:.1f} s"},
                 "parity": dict(allc["parity"], tolerance="max |d| <= 1 on RGBA8 (1/255), <= 1e-4 relative on RGBA32",
                                note="each oracle band against the same rows of the GPU frame of the same view")}
+    fl.free()
     view.free()
     tf.free()
     v.free()
@@ -1116,6 +1182,8 @@ def main():
                     choices=sorted(LEARNED_CASES) + ["batch_64x4", "serve_32"] + sorted(RENDER))
     ap.add_argument("--skip", default="learned", choices=["learned", "grid", "none"],
                     help="learned workloads: the skipping of the timed frames (learned grid by default)")
+    ap.add_argument("--inflight", type=int, default=3,
+                    help="frames in flight: consecutive frames alternate over this many views and streams")
     ap.add_argument("--no-certify", action="store_true",
                     help="learned workloads: learned grids without the cell-by-cell check against the exact test "
                          "(the per-frame judge alone guards the frames)")
@@ -1151,7 +1219,7 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if line is not None and world == 1 and args.workload == "learned_1024" and not args.no_extras:
         line["sorted_brick_512"] = _extra(run_sorted, args, [
-            "value", "unit", "gsamples_per_s", "kernel_ms", "e2e", "roofline", "sample_roofline", "plain_kernel",
+            "value", "unit", "gsamples_per_s", "frame_ms", "e2e", "roofline", "sample_roofline", "plain_kernel",
             "sampler_layouts", "samples", "other_macrocell_edges", "cpu_baseline", "config", "clocks"])
         line["batch_64x4"] = _extra(run_batch, args, ["value", "unit", "frames_per_s", "ms_per_step",
                                                       "megapixels_per_step", "autotune", "graph_replay", "config",
