@@ -357,7 +357,46 @@ def _learned_setup(ctx, L, vol, args):
     training = {"samples": n, "epochs": L["epochs"], "batch_rows": L["batch_rows"],
                 "loss_first": float(losses[0]), "loss_last": float(losses[-1]), "features_s": t_feat,
                 "train_s": t_train, "margin": margin, "recall_of_transparent_cells": recall}
-    return v, tfs, luts, mlp, training, ingest
+    return v, tfs, luts, mlp, training, ingest, margin
+
+
+def _uncertified(ctx, v, mlp, margin, tfs, states, L, args, stream):
+    """The same predictor and margin without the cell-by-cell certification
+    (the per-frame judge alone guarding the frames), every TF once with the
+    same views: frames/s, the judge's verdicts and the cells the network
+    called transparent that the exact test calls opaque.  The certified
+    grids are restored afterwards."""
+    import torch
+    from ivr_gb300 import api
+    w, h = L["image"]
+    sp = stream.cuda_stream
+    v.set_mlp(mlp, margin, certify=False)
+    view = ctx.view()
+    out = torch.empty((h, w, 4), dtype=torch.uint8, device="cuda")
+    p = api.config_params(step=L["step"], term_alpha=L["term"], skip=api.SKIP_LEARNED,
+                          judge_stride=args.judge_stride or L["judge_stride"])
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ms = 0.0
+    for t in range(len(tfs)):
+        view.set(v, states[t], p)
+        view.render(tfs[t], None, out.data_ptr(), sp)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(L["frames"]):
+            view.render(tfs[t], None, out.data_ptr(), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1) / L["frames"]
+    judge = view.judge_stats()
+    ls = v.learned_stats()
+    view.free()
+    v.set_mlp(mlp, margin, certify=True)
+    return {"fps": len(tfs) / (ms / 1000.0), "judge": judge, "false_skips": ls["false_skips"],
+            "learned_transparent": ls["learned_transparent"],
+            "note": "fallbacks = frames whose judged tiles (1 in judge_stride) differed by more than 1/255 from the "
+                    "exact grid's (worst = the largest 8-bit difference seen); such a frame is re-rendered with the "
+                    "exact grid and its TF's learned grid is not used again; frames whose judged tiles pass are "
+                    "not re-rendered"}
 
 
 def _methods(ctx, v, tfs, states, L, args, stream, device=0):
@@ -446,7 +485,7 @@ def run_learned(args, quiet=False):
     vol = workloads.learned_volume(L, device=f"cuda:{local}")
     torch.cuda.empty_cache()
     ctx = api.Context(local)
-    v, tfs, luts, mlp, training, ingest = _learned_setup(ctx, L, vol, args)
+    v, tfs, luts, mlp, training, ingest, margin = _learned_setup(ctx, L, vol, args)
     w, h = L["image"]
     ntf = len(tfs)
     stream = torch.cuda.Stream()
@@ -454,7 +493,11 @@ def run_learned(args, quiet=False):
     # the method comparison renders every TF once with each method (so each
     # TF's grids are resident before the timed region) on views of its own
     states = workloads.learned_views(L, n=max(ntf, args.steps + args.warmup), seed_offset=77 + 7919 * rank)
-    methods = None if args.no_methods else _methods(ctx, v, tfs, states, L, args, stream, local)
+    methods = None
+    if not args.no_methods:
+        methods = _methods(ctx, v, tfs, states, L, args, stream, local)
+        if not args.no_certify:
+            methods["uncertified"] = _uncertified(ctx, v, mlp, margin, tfs, states, L, args, stream)
 
     skip = {"learned": api.SKIP_LEARNED, "grid": api.SKIP_GRID, "none": api.SKIP_NONE}[args.skip]
     params = api.config_params(step=L["step"], term_alpha=L["term"], skip=skip,

@@ -284,19 +284,23 @@ int ivr_batch_set_variant(ivr_batch *batch, int variant);
 /* --- steering server: continuous batching over resident volumes ---------
  * Replaces the ivrserver/relay frame path (main.c:206-250,
  * myserver.c:133-165).  Clients submit requests at any time; a scheduler
- * thread keeps `slots` batches in flight, each on its own stream with an
- * output arena of arena_bytes taken from the context's HBM budget.  A free
- * slot takes the queued requests that fit (one volume dtype, outputs within
- * its arena) in arrival order and renders them in one batched launch (CONFIG
- * preset); requests arriving meanwhile wait and are admitted as slots and
- * arena memory free up.  Every frame equals ivr_render of the same view and
- * TF.  While a server runs, its context is used by the server's threads:
- * make no other calls on that context until ivr_server_destroy. */
+ * thread keeps `slots` batches in flight, each on its own stream.  The
+ * frames' device memory is one output pool of slots * arena_bytes taken from
+ * the context's HBM budget at creation.  A free slot takes the queued
+ * requests in arrival order, of any volume dtype, while their RGBA8 outputs
+ * fit the pool's largest free range (the HBM admission rule), and renders
+ * them (CONFIG preset; one batched launch per dtype among them); requests
+ * arriving meanwhile, or not fitting the free memory yet, wait and are
+ * admitted as slots and pool memory free up.  Only a frame larger than the
+ * whole pool is refused (IVR_ERR_NOMEM).  Every frame equals ivr_render of
+ * the same view and TF.  While a server runs, its context is used by the
+ * server's threads: make no other calls on that context until
+ * ivr_server_destroy. */
 typedef struct ivr_server ivr_server;
 typedef struct ivr_server_config {
     int slots;              /* batches in flight (streams), 1..16 */
     int max_batch_frames;   /* frames per batch */
-    size_t arena_bytes;     /* RGBA8 output memory per slot; larger frames are rejected */
+    size_t arena_bytes;     /* RGBA8 output memory per slot: the pool is slots * arena_bytes */
     int poll_us;            /* scheduler wake-up interval when idle */
     float step;             /* CONFIG sampling of every request */
     float term_alpha;
@@ -313,7 +317,7 @@ typedef struct ivr_request {
 } ivr_request;
 typedef struct ivr_completion {
     unsigned long long tag;
-    int status;               /* IVR_OK, IVR_ERR_NOMEM (frame larger than an arena), ... */
+    int status;               /* IVR_OK, IVR_ERR_NOMEM (frame larger than the output pool), ... */
     int vw, vh;
     double t_queue;           /* seconds from submit to the start of its batch */
     double t_total;           /* seconds from submit to the frame in host memory */

@@ -6,13 +6,16 @@
 // broadcast to MPI ranks and answered with one frame, many clients submit
 // requests (a resident volume, a STATE, a transfer function, an RGBA8 output
 // buffer) at any time.  A scheduler thread keeps several batch slots in
-// flight, each on its own stream with its own device output arena: whenever a
-// slot is free it takes the queued requests that fit (same volume dtype,
-// output bytes within the arena -- the HBM admission rule), renders them in one
-// persistent batched launch, copies the RGBA8 frames back and records
-// completion times.  Requests that arrive while slots are busy wait in the
-// queue and are admitted as slots and arena memory free up, so batches
-// overlap on the device.
+// flight, each on its own stream.  The frames' device memory is one output
+// pool taken from the context's HBM budget at start (slots x arena_bytes):
+// whenever a slot is free it takes the queued requests, in arrival order and
+// of any volume dtype, whose RGBA8 outputs fit the largest free range of the
+// pool -- the HBM admission rule -- renders them (one persistent batched
+// launch per dtype), copies the frames back and records completion times.
+// Requests that arrive while slots are busy, or that do not fit the free
+// memory yet, wait in the queue and are admitted as slots and pool memory
+// free up, so batches overlap on the device; only a frame larger than the
+// whole pool is refused.
 //
 // The optional TCP front end speaks the reference's steering protocol: a
 // client sends the 184-byte STATE (finish, winwidth, winheight in network
@@ -26,6 +29,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -62,8 +66,7 @@ struct Req {
 
 struct Slot {
     cudaStream_t stream = nullptr;
-    void *arena = nullptr;   // device RGBA8 outputs of one batch
-    void *pinned = nullptr;  // host staging of the same size
+    size_t base = 0, span = 0;  // its batch's range of the output pool (span 0: none)
     std::vector<ivr_view *> views;
     ivr_batch *batch[3] = {nullptr, nullptr, nullptr};  // per dtype
     cudaEvent_t ev = nullptr;
@@ -97,6 +100,13 @@ struct ivr_server {
     std::deque<Req> queue;
     std::deque<ivr_completion> done;
     std::vector<Slot> slots;
+    // the output pool: device RGBA8 frames of the batches in flight and
+    // their page-locked host staging, at the same offsets; ranges = the
+    // [offset, offset + bytes) the slots hold, under mu
+    void *pool = nullptr;
+    void *pool_pinned = nullptr;
+    size_t pool_bytes = 0;
+    std::vector<std::pair<size_t, size_t>> ranges;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::thread sched, copier;
@@ -123,6 +133,49 @@ struct ivr_server {
 namespace {
 
 int viewport_dim(int win, int tile) { return (win / tile) * tile; }
+
+// The output pool's free ranges, between the held ones (sorted by offset).
+// Under s->mu.  largest_free: the longest; first_fit: the offset of the
+// first at least `need` long, or pool_bytes when none is.
+size_t largest_free(const ivr_server *s)
+{
+    size_t at = 0, best = 0;
+    for (const auto &r : s->ranges) {
+        if (r.first > at) best = std::max(best, r.first - at);
+        at = std::max(at, r.first + r.second);
+    }
+    return std::max(best, s->pool_bytes > at ? s->pool_bytes - at : 0);
+}
+
+size_t first_fit(const ivr_server *s, size_t need)
+{
+    size_t at = 0;
+    for (const auto &r : s->ranges) {
+        if (r.first >= at + need) return at;
+        at = std::max(at, r.first + r.second);
+    }
+    return s->pool_bytes >= at + need ? at : s->pool_bytes;
+}
+
+void hold_range(ivr_server *s, Slot &sl, size_t off, size_t bytes)
+{
+    auto it = s->ranges.begin();
+    while (it != s->ranges.end() && it->first < off) ++it;
+    s->ranges.insert(it, {off, bytes});
+    sl.base = off;
+    sl.span = bytes;
+}
+
+void release_range(ivr_server *s, Slot &sl)
+{
+    if (sl.span == 0) return;
+    for (auto it = s->ranges.begin(); it != s->ranges.end(); ++it)
+        if (it->first == sl.base && it->second == sl.span) {
+            s->ranges.erase(it);
+            break;
+        }
+    sl.base = sl.span = 0;
+}
 
 void complete(ivr_server *s, Req &q, int status, double t_start)
 {
@@ -151,12 +204,13 @@ void finish_slot(ivr_server *s, Slot &sl)
     const double batch_s = cudaEventElapsedTime(&ms, sl.t0, sl.t1) == cudaSuccess ? ms / 1000.0 : 0.0;
     for (size_t i = 0; i < sl.reqs.size(); i++) {
         Req &q = sl.reqs[i];
-        if (!q.direct) memcpy(q.r.rgba8_host, (char *) sl.pinned + sl.offs[i], q.bytes);
+        if (!q.direct) memcpy(q.r.rgba8_host, (char *) s->pool_pinned + sl.base + sl.offs[i], q.bytes);
         complete(s, q, IVR_OK, sl.t_start);
     }
     sl.reqs.clear();
     sl.offs.clear();
     std::lock_guard<std::mutex> lock(s->mu);
+    release_range(s, sl);
     sl.busy = false;
     s->gpu_s += batch_s;  // read under the same lock by ivr_server_times
     s->finish_s += now_s() - t;
@@ -201,89 +255,105 @@ void materialise_tfs(ivr_server *s)
     }
 }
 
-// takes the queued requests that fit a free slot and launches them
+// takes the queued requests that fit a free slot and the free output
+// memory, and launches them
 bool dispatch(ivr_server *s, Slot &sl)
 {
     std::vector<Req> take, never;
     {
         std::lock_guard<std::mutex> lock(s->mu);
         if (s->queue.empty()) return false;
-        const int dtype = s->queue.front().dtype;
+        const size_t room = largest_free(s);
         size_t used = 0;
         for (auto it = s->queue.begin(); it != s->queue.end() && (int) take.size() < s->cfg.max_batch_frames;) {
-            if (it->bytes > s->cfg.arena_bytes) {  // larger than an arena: never admitted
+            if (it->bytes > s->pool_bytes) {  // larger than the whole pool: never admitted
                 never.push_back(*it);
                 it = s->queue.erase(it);
                 continue;
             }
-            if (it->dtype != dtype) {
-                ++it;
-                continue;
-            }
-            if (used + it->bytes > s->cfg.arena_bytes) break;  // arrival order: wait for the next slot
+            if (used + it->bytes > room) break;  // arrival order: wait for memory to free up
             used += it->bytes;
             take.push_back(*it);
             it = s->queue.erase(it);
         }
+        if (!take.empty()) hold_range(s, sl, first_fit(s, used), used);
     }
     for (auto &q : never) complete(s, q, IVR_ERR_NOMEM, 0.0);
     if (take.empty()) return !never.empty();
-    const int dtype = take[0].dtype;
-    ivr_batch *&b = sl.batch[dtype];
-    if (!b) {
-        if (ivr_batch_create(s->ctx, s->cfg.max_batch_frames, &b) != IVR_OK) b = nullptr;
-        else ivr_batch_set_variant(b, s->cfg.variant);
-    }
     sl.t_start = now_s();
-    size_t off = 0;
-    std::vector<Req> ok;
-    if (b) ivr_batch_clear(b);
     for (auto &q : take)
         if (q.r.tf >= (int) s->tfs.size() || (q.r.tf >= 0 && !s->tfs[q.r.tf])) {
             materialise_tfs(s);  // registered after the last pass
             break;
         }
-    for (auto &q : take) {
-        ivr_view *view = sl.views[ok.size()];
-        ivr_tf *tf = (q.r.tf >= 0 && q.r.tf < (int) s->tfs.size()) ? s->tfs[q.r.tf] : nullptr;
-        int rc = b ? IVR_OK : IVR_ERR_NOMEM;
-        if (rc == IVR_OK && !tf) rc = IVR_ERR_INVALID;
-        if (rc == IVR_OK) rc = ivr_set_view(view, q.vol, &q.r.state, &s->params);
-        if (rc == IVR_OK) rc = ivr_batch_add(b, view, tf, nullptr, (uint8_t *) sl.arena + off);
-        if (rc != IVR_OK) {
-            complete(s, q, rc, sl.t_start);
-            continue;
-        }
-        sl.offs.push_back(off);
-        off += q.bytes;
-        ok.push_back(q);
-    }
-    if (ok.empty()) return true;
+    char *const dev = (char *) s->pool + sl.base;
+    size_t off = 0;
+    std::vector<Req> ok;
     cudaEventRecord(sl.t0, sl.stream);
-    int rc = ivr_batch_render(b, 1, sl.stream);
+    int rc = IVR_OK;
+    // one batched launch per volume dtype among the requests taken
+    for (int dtype = IVR_U8; dtype <= IVR_F32 && rc == IVR_OK; dtype++) {
+        ivr_batch *&b = sl.batch[dtype];
+        size_t nd = 0;
+        for (auto &q : take) nd += q.dtype == dtype;
+        if (nd == 0) continue;
+        if (!b) {
+            if (ivr_batch_create(s->ctx, s->cfg.max_batch_frames, &b) != IVR_OK) b = nullptr;
+            else ivr_batch_set_variant(b, s->cfg.variant);
+        }
+        if (b) ivr_batch_clear(b);
+        size_t added = 0;
+        for (auto &q : take) {
+            if (q.dtype != dtype) continue;
+            ivr_view *view = sl.views[ok.size()];
+            ivr_tf *tf = (q.r.tf >= 0 && q.r.tf < (int) s->tfs.size()) ? s->tfs[q.r.tf] : nullptr;
+            int qrc = b ? IVR_OK : IVR_ERR_NOMEM;
+            if (qrc == IVR_OK && !tf) qrc = IVR_ERR_INVALID;
+            if (qrc == IVR_OK) qrc = ivr_set_view(view, q.vol, &q.r.state, &s->params);
+            if (qrc == IVR_OK) qrc = ivr_batch_add(b, view, tf, nullptr, (uint8_t *) dev + off);
+            if (qrc != IVR_OK) {
+                complete(s, q, qrc, sl.t_start);
+                continue;
+            }
+            sl.offs.push_back(off);
+            off += q.bytes;
+            ok.push_back(q);
+            added++;
+        }
+        if (added) rc = ivr_batch_render(b, 1, sl.stream);
+    }
+    if (ok.empty()) {
+        std::lock_guard<std::mutex> lock(s->mu);
+        release_range(s, sl);
+        return true;
+    }
     if (rc == IVR_OK) cudaEventRecord(sl.t1, sl.stream);
     // frames for page-locked buffers go straight there; the others through
-    // the slot's staging, one copy per run of consecutive staged frames
+    // the pool's staging, one copy per run of consecutive staged frames
     for (size_t i = 0; i < ok.size() && rc == IVR_OK;) {
         const size_t o = sl.offs[i];
         if (ok[i].direct) {
-            if (cudaMemcpyAsync(ok[i].r.rgba8_host, (char *) sl.arena + o, ok[i].bytes, cudaMemcpyDeviceToHost,
-                                sl.stream) != cudaSuccess)
+            if (cudaMemcpyAsync(ok[i].r.rgba8_host, dev + o, ok[i].bytes, cudaMemcpyDeviceToHost, sl.stream) !=
+                cudaSuccess)
                 rc = IVR_ERR_CUDA;
             i++;
             continue;
         }
         size_t j = i, end = o;
         while (j < ok.size() && !ok[j].direct) end = sl.offs[j] + ok[j].bytes, j++;
-        if (cudaMemcpyAsync((char *) sl.pinned + o, (char *) sl.arena + o, end - o, cudaMemcpyDeviceToHost,
+        if (cudaMemcpyAsync((char *) s->pool_pinned + sl.base + o, dev + o, end - o, cudaMemcpyDeviceToHost,
                             sl.stream) != cudaSuccess)
             rc = IVR_ERR_CUDA;
         i = j;
     }
     if (rc == IVR_OK && cudaEventRecord(sl.ev, sl.stream) != cudaSuccess) rc = IVR_ERR_CUDA;
     if (rc != IVR_OK) {
+        // nothing of this batch may still write the range it releases
+        cudaStreamSynchronize(sl.stream);
         for (auto &q : ok) complete(s, q, rc, sl.t_start);
         sl.offs.clear();
+        std::lock_guard<std::mutex> lock(s->mu);
+        release_range(s, sl);
         return true;
     }
     sl.reqs = std::move(ok);
@@ -500,16 +570,21 @@ int ivr_server_create(ivr_ctx *ctx, const ivr_server_config *cfg, ivr_server **o
     s->params.tileh = c.tileh;
     s->slots.resize(c.slots);
     int rc = IVR_OK;
+    // the output pool comes out of the context's HBM budget
+    s->pool_bytes = c.arena_bytes * (size_t) c.slots;
+    if (cudaMallocHost(&s->pool_pinned, s->pool_bytes) != cudaSuccess) {
+        s->pool_pinned = nullptr;
+        rc = IVR_ERR_NOMEM;
+    }
+    if (rc == IVR_OK && (rc = ivr_device_alloc(ctx, s->pool_bytes, &s->pool)) != IVR_OK) s->pool = nullptr;
     for (auto &sl : s->slots) {
-        // the output arenas come out of the context's HBM budget
+        if (rc != IVR_OK) break;
         if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreate(&sl.t0) != cudaSuccess || cudaEventCreate(&sl.t1) != cudaSuccess ||
-            cudaMallocHost(&sl.pinned, c.arena_bytes) != cudaSuccess) {
+            cudaEventCreate(&sl.t0) != cudaSuccess || cudaEventCreate(&sl.t1) != cudaSuccess) {
             rc = IVR_ERR_CUDA;
             break;
         }
-        if ((rc = ivr_device_alloc(ctx, c.arena_bytes, &sl.arena)) != IVR_OK) break;
         sl.views.resize(c.max_batch_frames, nullptr);
         for (auto &v : sl.views)
             if ((rc = ivr_view_create(ctx, &v)) != IVR_OK) break;
@@ -660,13 +735,13 @@ int ivr_server_destroy(ivr_server *s)
             if (b) ivr_batch_free(b);
         for (auto *v : sl.views)
             if (v) ivr_view_free(v);
-        if (sl.arena) ivr_device_free(s->ctx, sl.arena, s->cfg.arena_bytes);
-        if (sl.pinned) cudaFreeHost(sl.pinned);
         if (sl.ev) cudaEventDestroy(sl.ev);
         if (sl.t0) cudaEventDestroy(sl.t0);
         if (sl.t1) cudaEventDestroy(sl.t1);
         if (sl.stream) cudaStreamDestroy(sl.stream);
     }
+    if (s->pool) ivr_device_free(s->ctx, s->pool, s->pool_bytes);
+    if (s->pool_pinned) cudaFreeHost(s->pool_pinned);
     for (auto *tf : s->tfs)
         if (tf) ivr_tf_free(tf);
     delete s;

@@ -1,6 +1,8 @@
 """GPU: the steering server.  Each frame served in a mix of concurrent
 requests (different volumes, dtypes, sizes, TFs) equals the frame rendered
-alone; oversized frames are rejected without stopping the server; the TCP
+alone; a frame larger than one slot's share of the output pool waits for
+memory and is served, one larger than the pool is rejected without
+stopping the server; the TCP
 front end speaks the reference's STATE/RGBA8 protocol and survives clients
 that disconnect mid-message."""
 import socket
@@ -87,6 +89,38 @@ def test_oversized_request_is_rejected(vols):
     srv.close()
     st = {r["tag"]: r["status"] for r in got}
     assert st[1] == -3 and st[2] == 0
+
+
+def test_pool_admits_a_frame_larger_than_one_arena(vols):
+    """The output pool is slots x arena_bytes, shared: a frame larger than
+    one slot's share waits for pool memory and is served; only a frame
+    larger than the whole pool is refused.  Requests of the three volume
+    dtypes share batches."""
+    ctx, vs = vols
+    srv = api.Server(ctx, slots=4, max_batch_frames=8, arena_mib=1)  # a 4 MiB pool
+    ids = [srv.add_volume(v) for v, _ in vs]
+    luts = [synth.knot_tf(40 + k)[0] for k in range(3)]
+    tfs = [srv.add_tf(luts[k], 0, vs[k][1]) for k in range(3)]
+    sizes = [(64, 48), (1024, 768), (80, 80), (1100, 1000), (48, 64), (512, 512)]  # 3 MiB; 4.4 MB > pool
+    reqs = {}
+    for tag, (w, h) in enumerate(sizes * 2):
+        k = tag % 3
+        st = orbit_state(20.0 + 37 * tag, 10.0, w, h, fovy=30.0, alpha=1.0)
+        srv.submit(ids[k], tfs[k], st, tag)
+        reqs[tag] = (k, st, w * h * 4)
+    done = []
+    while len(done) < len(reqs):
+        done.extend(srv.poll(wait_ms=200))
+    stats = srv.stats()
+    srv.close()
+    for r in done:
+        k, st, nbytes = reqs[r["tag"]]
+        if nbytes > 4 << 20:
+            assert r["status"] == -3, r
+            continue
+        assert r["status"] == 0, r
+        assert np.array_equal(r["frame"], render_alone(ctx, vs[k][0], luts[k], vs[k][1], st)), r["tag"]
+    assert stats["rejected"] == 2 and stats["completed"] == len(reqs) - 2
 
 
 def state_bytes(st):
