@@ -103,6 +103,7 @@ static ivr_ctx *ctx; static ivr_volume *vol; static ivr_view *view; static ivr_t
 static ivr_view *views[4]; static ivr_tf *tfs[4]; static ivr_tf *train_tfs[4];
 static uint8_t *rgba8_dev[4]; static ivr_state state; static ivr_render_params params;
 static void *stream; static int nframes, ntrain, w, h;
+static ivr_state states[8];
 static const float *rgba;
 """
 
