@@ -495,9 +495,12 @@ def run_learned(args, quiet=False):
     states = workloads.learned_views(L, n=max(ntf, args.steps + args.warmup), seed_offset=77 + 7919 * rank)
     methods = None
     if not args.no_methods:
+        # the uncertified grids first: re-attaching the predictor drops a
+        # volume's learned grids, which the comparison then builds again
+        unc = None if args.no_certify else _uncertified(ctx, v, mlp, margin, tfs, states, L, args, stream)
         methods = _methods(ctx, v, tfs, states, L, args, stream, local)
-        if not args.no_certify:
-            methods["uncertified"] = _uncertified(ctx, v, mlp, margin, tfs, states, L, args, stream)
+        if unc is not None:
+            methods["uncertified"] = unc
 
     skip = {"learned": api.SKIP_LEARNED, "grid": api.SKIP_GRID, "none": api.SKIP_NONE}[args.skip]
     params = api.config_params(step=L["step"], term_alpha=L["term"], skip=skip,
@@ -515,10 +518,11 @@ def run_learned(args, quiet=False):
 
     timed_ks = range(args.warmup, nsteps)
     with torch.cuda.stream(stream):
-        if methods is None:  # every TF's grids built before the timed region, as the comparison does
-            for t in sorted({t for _, t in frames}):
-                view.set(v, frames[0][0], params)
-                view.render(tfs[t], None, fl.dev[0].data_ptr(), sp)
+        # every TF's grids built before the timed region (the comparison has
+        # built them already when it ran)
+        for t in sorted({t for _, t in frames}):
+            view.set(v, frames[0][0], params)
+            view.render(tfs[t], None, fl.dev[0].data_ptr(), sp)
         for k in range(args.warmup):
             frame(k)
         torch.cuda.synchronize()
