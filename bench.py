@@ -308,9 +308,11 @@ def learned_config(args, L):
             "image": f"{w}x{h}", "tfs": f"{L['tfs']} random 16-knot piecewise-linear TFs, 60% zero opacity knots",
             "lut": "256-entry RGBA FP32, index (int)(v*256/65536)",
             "step_voxels": L["step"], "early_termination_alpha": L["term"],
-            "skip": {"learned": f"learned grid (26-64-64-1 BF16 MLP, trained on {L['train_tfs']} TFs), judged 1 "
+            "macrocell_voxels": getattr(args, "cell", 16),
+            "skip": {"learned": f"learned grid (26-64-64-1 BF16 MLP, trained on "
+                                f"{getattr(args, 'train_tfs', 0) or L['train_tfs']} TFs), judged 1 "
                                 f"tile in {L['judge_stride']} at 1/255 with exact-grid fallback",
-                     "grid": "exact macrocell grid of 16^3-voxel cells",
+                     "grid": "exact macrocell grid",
                      "none": "none (every lattice point)"}[getattr(args, "skip", "learned")],
             "step": "one frame: a new view under the next TF",
             "frames_in_flight": getattr(args, "inflight", 3),
@@ -321,6 +323,8 @@ def _learned_setup(ctx, L, vol, args):
     """Ingestion through the streamed file load, the TFs, and the predictor
     trained on the device: (volume, tf handles, luts, training summary)."""
     from ivr_gb300 import api
+    if int(os.environ.get("RANK", "0")) != 0:  # replicas: one temporary volume file per job is enough
+        return _learned_train(ctx, L, ctx.load_volume(vol), args, {"source": "host memory (ivr_volume_load)"})
     ingest = {"bytes": int(vol.nbytes), "source": "raw little-endian file in the page cache"}
     v = None
     try:
@@ -338,13 +342,21 @@ def _learned_setup(ctx, L, vol, args):
     except OSError as e:
         ingest["error"] = str(e)
         v = ctx.load_volume(vol)
+    return _learned_train(ctx, L, v, args, ingest)
+
+
+def _learned_train(ctx, L, v, args, ingest):
+    """The TFs and the predictor trained on the device for volume v."""
+    from ivr_gb300 import api
+    if args.linear or args.cell != 16:  # the layout and cells the predictor is trained on
+        v.quads(not args.linear).macrocell(args.cell)
     luts = workloads.learned_tfs(L)
     scale = workloads.lut_scale(L["dtype"])
     tfs = [ctx.transfer_function().set_lut(t, 0, scale, api.TF_F2B) for t in luts]
     mlp = ctx.mlp(L["seed"])
     t0 = time.perf_counter()
     n = 0
-    for tf in tfs[:L["train_tfs"]]:
+    for tf in tfs[:args.train_tfs or L["train_tfs"]]:
         n = mlp.add_samples(v, tf)
     t_feat = time.perf_counter() - t0
     t0 = time.perf_counter()
@@ -352,8 +364,6 @@ def _learned_setup(ctx, L, vol, args):
     t_train = time.perf_counter() - t0
     margin, recall = mlp.calibrate(L["slack"])
     v.set_mlp(mlp, margin, certify=not args.no_certify)
-    if args.linear or args.cell != 16:
-        v.quads(not args.linear).macrocell(args.cell)
     training = {"samples": n, "epochs": L["epochs"], "batch_rows": L["batch_rows"],
                 "loss_first": float(losses[0]), "loss_last": float(losses[-1]), "features_s": t_feat,
                 "train_s": t_train, "margin": margin, "recall_of_transparent_cells": recall}
@@ -1229,6 +1239,8 @@ def main():
                     choices=sorted(LEARNED_CASES) + ["batch_64x4", "serve_32"] + sorted(RENDER))
     ap.add_argument("--skip", default="learned", choices=["learned", "grid", "none"],
                     help="learned workloads: the skipping of the timed frames (learned grid by default)")
+    ap.add_argument("--train-tfs", type=int, default=0,
+                    help="learned workloads: TFs whose cells train the predictor (0: the workload's 8)")
     ap.add_argument("--inflight", type=int, default=3,
                     help="frames in flight: consecutive frames alternate over this many views and streams")
     ap.add_argument("--no-certify", action="store_true",
