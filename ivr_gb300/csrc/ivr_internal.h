@@ -44,9 +44,10 @@ struct DevBrick {
                             // input; or null
 };
 
-// Learned-skip judge words of a view (device).  maxdiff and warps_done are
-// per-frame scratch the judged launch clears after use; fail is the last
-// frame's verdict (the fallback launch's gate); the rest are running totals.
+// Learned-skip judge words of a view (device).  maxdiff and warps_done (the
+// compare launch's blocks done) are per-frame scratch the compare launch
+// clears after use; fail is the last frame's verdict (the fallback launch's
+// gate); the rest are running totals.
 struct JudgeWords {
     int maxdiff;
     int warps_done;

@@ -842,25 +842,39 @@ struct JudgeArgs {
     int judge_tol;
 };
 
-// End of a judge launch for one warp: its largest difference and pixel
-// count go into the judge words; the launch's last warp sets the verdict
-// (fail = largest difference > tolerance), adds it to the totals, marks the
-// learned grid wrong on failure and clears the per-frame words.  A grid
-// already marked wrong was not used (the frame marched with the exact
-// grid): nothing is judged and the frame counts as an exact one.
+// End of a judge launch for one block: the largest difference and pixel
+// count of its warps go into the judge words (one set of atomics per block,
+// not per warp: thousands of warps updating the same words would serialise
+// on them); the launch's last block sets the verdict (fail = largest
+// difference > tolerance), adds it to the totals, marks the learned grid
+// wrong on failure and clears the per-frame words.  A grid already marked
+// wrong was not used (the frame marched with the exact grid): nothing is
+// judged and the frame counts as an exact one.  Every thread of the block
+// calls it.
 __device__ __forceinline__ void judge_finish(const JudgeArgs &a, int worst, unsigned judged, bool known_bad)
 {
+    __shared__ int b_worst;
+    __shared__ unsigned b_judged;
+    if (threadIdx.x == 0) {
+        b_worst = 0;
+        b_judged = 0;
+    }
+    __syncthreads();
     for (int o = 16; o > 0; o >>= 1) {
         worst = max(worst, __shfl_xor_sync(0xffffffffu, worst, o));
         judged += __shfl_xor_sync(0xffffffffu, judged, o);
     }
-    if ((threadIdx.x & 31) != 0) return;
+    if ((threadIdx.x & 31) == 0) {
+        if (worst > 0) atomicMax_block(&b_worst, worst);
+        if (judged) atomicAdd_block(&b_judged, judged);
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     JudgeWords *jw = a.judge;
-    if (worst > 0) atomicMax(&jw->maxdiff, worst);
-    if (judged) atomicAdd(&jw->pixels, (unsigned long long) judged);
+    if (b_worst > 0) atomicMax(&jw->maxdiff, b_worst);
+    if (b_judged) atomicAdd(&jw->pixels, (unsigned long long) b_judged);
     __threadfence();
-    const int warps = (int) gridDim.x * (int) (blockDim.x >> 5);
-    if (atomicAdd(&jw->warps_done, 1) != warps - 1) return;
+    if (atomicAdd(&jw->warps_done, 1) != (int) gridDim.x - 1) return;  // counts blocks
     __threadfence();
     const int m = atomicAdd(&jw->maxdiff, 0);
     const int failed = m > a.judge_tol;
@@ -909,8 +923,10 @@ __global__ void __launch_bounds__(kThreads, JUDGE ? kJudgeBlocksPerSm : kCfgBloc
     const int tiles_x = (f.out_w + 7) >> 3;
     const long long ntiles = (long long) tiles_x * ((f.out_h + 3) >> 2);
     if (f.gate != nullptr && *f.gate == 0) {
-        const bool first = blockIdx.x == 0 && threadIdx.x == 0;
-        if (lane == 0) atomicAdd(f.tickets, first ? (unsigned long long) ntiles + 1ull : 1ull);
+        // no fallback: the launch's share of tickets (every tile, and one
+        // failed take per warp) in one add instead of one per warp
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            atomicAdd(f.tickets, (unsigned long long) ntiles + (unsigned long long) gridDim.x * (blockDim.x >> 5));
         return;
     }
     const bool exact = JUDGE && *(volatile const int *) f.learned_bad != 0;
