@@ -538,3 +538,41 @@ def test_sampler_layouts(ctx, dtype):
     assert g > 0 and 0.0 < err < 0.01 * full
     with pytest.raises(Exception):
         ctx.sample_peak_layout(dtype, 4)
+
+
+@pytest.mark.parametrize("case", ["camera_inside", "one_pixel", "all_zero", "tiny_volume"])
+def test_config_edge_cases_match_o2(ctx, oracle_mod, case):
+    """Edge cases against O2, bit for bit, with and without skipping: the
+    camera inside the volume (rays start at t = 0 inside the box), a 1x1
+    window, a volume of zeros (every cell transparent: nothing is sampled),
+    and the smallest volume with bricks (2^3 voxels, one cell)."""
+    shape, dtype, procdims, win, dist = (40, 40, 40), "u8", (2, 2, 2), (64, 48), 5.0
+    vol = make_config_volume(shape, dtype, 23)
+    if case == "camera_inside":
+        dist = 0.3
+    elif case == "one_pixel":
+        win = (1, 1)
+    elif case == "all_zero":
+        vol = np.zeros(shape, np.uint8)
+    elif case == "tiny_volume":
+        vol = (np.arange(8, dtype=np.uint8).reshape(2, 2, 2) * 30 + 40)
+        procdims = (1, 1, 1)
+    st = orbit_state(37, 21, win[0], win[1], fovy=30.0, alpha=1.0, dist=dist)
+    lut = synth.ramp_tf(256)
+    ref = oracle_mod.render(vol, st, lut, 0, 6, preset=1, procdims=procdims)
+    v = ctx.load_volume(vol)
+    if np.prod(procdims) > 1:
+        v.bricks(*procdims)
+    tf = ctx.transfer_function().set_lut(lut, 0, 1.0, api.TF_F2B)
+    for skip in (False, True):
+        view = ctx.view().set(v, st, api.config_params(skip=skip))
+        o32, o8 = dev_frame(win[1], win[0])
+        view.render(tf, o32.data_ptr(), o8.data_ptr())
+        assert np.array_equal(bits(host(o32)), bits(ref["rgba32"])), (case, skip)
+        assert np.array_equal(host(o8), ref["rgba8"]), (case, skip)
+        view.free()
+    if case == "all_zero":
+        assert not ref["rgba32"].any()
+    if case == "camera_inside":
+        assert ref["rgba32"][..., 3].max() > 0
+    v.free()
