@@ -38,6 +38,7 @@ struct ivr_mlp {
     long long scap = 0;
     float *d_knots = nullptr;
     int *d_key = nullptr;
+    int *d_status = nullptr;  // inference status word (kMlpTcTimeout)
     unsigned long long *d_counts = nullptr;
     cudaEvent_t scratch_ev = nullptr;  // after the last use of the scratch
 };
@@ -58,6 +59,7 @@ MlpDev dev_of(const ivr_mlp *m)
     w.b2 = m->d_p + kOffB2;
     w.w3 = m->d_p + kOffW3;
     w.b3 = m->d_p + kOffB3;
+    w.status = m->d_status;
     return w;
 }
 
@@ -223,6 +225,7 @@ int ivr_mlp_free(ivr_mlp *m)
     dev_free(c, m->d_ys, (size_t) m->scap * sizeof(float));
     dev_free(c, m->d_knots, kMlpKnots * sizeof(float));
     dev_free(c, m->d_key, sizeof(int));
+    dev_free(c, m->d_status, sizeof(int));
     dev_free(c, m->d_counts, 2 * sizeof(unsigned long long));
     if (m->scratch_ev) cudaEventDestroy(m->scratch_ev);
     delete m;
@@ -245,6 +248,9 @@ int ivr_mlp_create(ivr_ctx *c, unsigned long long seed, ivr_mlp **out)
     if (rc == IVR_OK) rc = dev_alloc(c, (size_t) kMlpHidden * kMlpHidden * kBf16Bytes, &m->d_w2);
     if (rc == IVR_OK) rc = dev_alloc(c, kMlpKnots * sizeof(float), (void **) &m->d_knots);
     if (rc == IVR_OK) rc = dev_alloc(c, sizeof(int), (void **) &m->d_key);
+    if (rc == IVR_OK) rc = dev_alloc(c, sizeof(int), (void **) &m->d_status);
+    if (rc == IVR_OK && cudaMemset(m->d_status, 0, sizeof(int)) != cudaSuccess)
+        rc = fail(c, IVR_ERR_CUDA, "predictor status");
     if (rc == IVR_OK) rc = dev_alloc(c, 2 * sizeof(unsigned long long), (void **) &m->d_counts);
     if (rc == IVR_OK && cudaEventCreateWithFlags(&m->scratch_ev, cudaEventDisableTiming) != cudaSuccess)
         rc = fail(c, IVR_ERR_CUDA, "predictor event");
@@ -483,6 +489,12 @@ int ivr_mlp_calibrate(ivr_mlp *m, float slack, float *margin, float *recall)
     CK(c, cudaMemset(m->d_counts, 0, sizeof(counts)));
     CK(c, mlp_calibrate(m->d_Y, m->d_T, m->n, mg, m->d_key, m->d_counts, 0));
     CK(c, cudaMemcpy(counts, m->d_counts, sizeof(counts), cudaMemcpyDeviceToHost));
+    int status = 0;
+    CK(c, cudaMemcpy(&status, m->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status != 0) {
+        cudaMemset(m->d_status, 0, sizeof(int));
+        return fail(c, IVR_ERR_TIMEOUT, "a tensor-core wait of the predictor's inference ran out");
+    }
     *margin = mg;
     if (recall) *recall = counts[0] ? (float) ((double) counts[1] / (double) counts[0]) : 0.0f;
     return IVR_OK;

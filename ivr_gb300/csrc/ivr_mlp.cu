@@ -1,8 +1,9 @@
 // ivr_mlp.cu -- the learned empty-space predictor: a 26 -> 64 -> 64 -> 1 MLP
 // (BF16 weights and activations, FP32 accumulation) on the tensor cores with
-// mma.sync.m16n8k16, its training step (forward + backward in one kernel per
-// 128-row tile, weight gradients accumulated in FP32), Adam, and the
-// per-macrocell features and targets it learns from.
+// mma.sync.m16n8k16 for its training step (forward + backward in one kernel
+// per 128-row tile, weight gradients accumulated in FP32), Adam, and the
+// per-macrocell features and targets it learns from.  Inference runs on the
+// tcgen05 tensor cores (ivr_mlp_tc.cu).
 //
 // Fragment layouts of mma.m16n8k16 (row.col, bf16 -> f32), per lane with
 // g = lane / 4 and t = lane % 4:
@@ -161,26 +162,6 @@ __device__ void output_rows(const FwdSmem &s, const float (&h2)[2][8][4], float 
             p += __shfl_xor_sync(0xffffffffu, p, 2);
             y[mt][hi] = p + b3;
         }
-}
-
-__global__ void __launch_bounds__(R) mlp_forward_kernel(MlpDev w, const bf16 *X, long long n, float *y)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    FwdSmem &s = *reinterpret_cast<FwdSmem *>(smem_raw);
-    const long long row0 = (long long) blockIdx.x * R;
-    load_tile<false>(s, nullptr, w, X, nullptr, row0, n);
-    __syncthreads();
-    float h2[2][8][4];
-    forward_rows<false>(s, nullptr, h2);
-    float yy[2][2];
-    output_rows(s, h2, *w.b3, yy);
-    const int warp = threadIdx.x >> 5, g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-    if (t == 0)
-        for (int mt = 0; mt < 2; mt++)
-            for (int hi = 0; hi < 2; hi++) {
-                const long long row = row0 + warp * 32 + 16 * mt + g + 8 * hi;
-                if (row < n) y[row] = yy[mt][hi];
-            }
 }
 
 // Forward and backward of one 128-row tile of rows idx[0..n) (or 0..n).
@@ -521,14 +502,7 @@ size_t mlp_train_smem() { return sizeof(BwdSmem); }
 
 cudaError_t mlp_forward(const MlpDev &w, const void *X, long long n, float *y, cudaStream_t s)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sizeof(FwdSmem));
-        attr = true;
-    }
-    if (n <= 0) return cudaSuccess;
-    mlp_forward_kernel<<<(unsigned) ((n + R - 1) / R), R, sizeof(FwdSmem), s>>>(w, (const bf16 *) X, n, y);
-    return cudaGetLastError();
+    return mlp_forward_tc(w, X, n, y, w.status, s);
 }
 
 cudaError_t mlp_train_step(const MlpDev &w, const void *X, const float *T, const int *idx, long long n,

@@ -30,11 +30,15 @@ struct MlpDev {
     const void *w2t;  // bf16 [hidden out][hidden in]
     const void *w2;   // bf16 [hidden in][hidden out]
     const float *b1, *b2, *w3, *b3;
+    int *status;      // inference: kMlpTcTimeout when a tensor-core wait ran out (else untouched)
 };
+constexpr int kMlpTcTimeout = 1;
 
 size_t mlp_forward_smem();
 size_t mlp_train_smem();
+// inference: y for rows 0..n of X, on the tcgen05 tensor cores (ivr_mlp_tc.cu)
 cudaError_t mlp_forward(const MlpDev &w, const void *X, long long n, float *y, cudaStream_t s);
+cudaError_t mlp_forward_tc(const MlpDev &w, const void *X, long long n, float *y, int *status, cudaStream_t s);
 // forward + backward over rows idx[0..n) (idx null: rows 0..n), gradients
 // added into grad, loss into *loss; targets <= 0 are one-sided (gamma)
 cudaError_t mlp_train_step(const MlpDev &w, const void *X, const float *T, const int *idx, long long n,

@@ -1,0 +1,271 @@
+// ivr_mlp_tc.cu -- inference of the learned empty-space predictor on the
+// 5th-generation tensor cores (tcgen05): a 128-row tile of features X
+// [128 x 32] times W1 [32 x 64] and the hidden layer H1 [128 x 64] times W2
+// [64 x 64], BF16 operands in shared memory, FP32 accumulators in tensor
+// memory (TMEM), one elected thread issuing the MMAs, an mbarrier signalled
+// by tcgen05.commit, and the epilogues (bias, ReLU, the last layer's dot
+// product) on the accumulators read back with tcgen05.ld: TMEM lane r holds
+// tile row r, so every thread finishes its own row.
+//
+// Shared-memory operands use the canonical K-major layout without swizzle:
+// 8-row x 16-byte core matrices, the K-adjacent ones 128 bytes apart (the
+// descriptor's leading byte offset) and the row-adjacent ones SBO bytes
+// apart (the stride byte offset: K/8 core matrices of 128 bytes).  Element
+// (r, k) of such a tile lies at (r/8)*SBO + (k/8)*128 + (r%8)*16 + (k%8)*2.
+//
+// Every wait is bounded; a wait that runs out records kMlpTcTimeout in
+// *status, waits (bounded) for the MMAs in flight, frees the tile's TMEM and
+// leaves the rows unwritten; the caller turns the status into an error.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "ivr_internal.h"
+#include "ivr_mlp.h"
+
+namespace ivr {
+namespace {
+
+using bf16 = __nv_bfloat16;
+constexpr int kIn = kMlpIn;       // 32
+constexpr int kHid = kMlpHidden;  // 64
+constexpr int kRows = 128;        // M of one MMA tile, one row per thread
+constexpr int kSbo1 = (kIn / 8) * 128;   // 512: X and W1 tiles (K = 32)
+constexpr int kSbo2 = (kHid / 8) * 128;  // 1024: H1 and W2 tiles (K = 64)
+constexpr uint32_t kTmemCols = 128;      // D1 in columns 0-63, D2 in 64-127
+constexpr long long kWaitLimit = 1ll << 24;
+
+struct TcSmem {
+    alignas(128) unsigned char x[kRows * kIn * 2];   // 8 KB, A of layer 1
+    alignas(128) unsigned char w1[kHid * kIn * 2];   // 4 KB, B of layer 1 (W1t: n x k)
+    alignas(128) unsigned char h1[kRows * kHid * 2]; // 16 KB, A of layer 2
+    alignas(128) unsigned char w2[kHid * kHid * 2];  // 8 KB, B of layer 2 (W2t: n x k)
+    float b1[kHid], b2[kHid], w3[kHid];
+    unsigned long long mbar;
+    uint32_t tmem;
+};
+// dynamic shared memory asked per block: above TcSmem, so that at most four
+// blocks share an SM and their 4 x 128 TMEM columns fit its 512
+constexpr size_t kTcSmemBytes = 56 * 1024;
+static_assert(sizeof(TcSmem) <= kTcSmemBytes, "smem");
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t) __cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ int kmajor_off(int r, int k, int sbo) { return (r >> 3) * sbo + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2; }
+
+// shared-memory matrix descriptor: start, leading byte offset (K-adjacent
+// core matrices), stride byte offset (row-adjacent), descriptor version 1,
+// no swizzle
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t) ((saddr >> 4) & 0x3fffu) | ((uint64_t) ((lbo >> 4) & 0x3fffu) << 16) |
+           ((uint64_t) ((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3, M >> 4
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t) (n >> 3) << 17) | ((uint32_t) (m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+// bounded wait for phase `parity` of the mbarrier; false when it ran out
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+{
+    for (long long it = 0; it < kWaitLimit; it++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b)
+{
+    const bf16 lo = __float2bfloat16(a), hi = __float2bfloat16(b);
+    return (uint32_t) __bfloat16_as_ushort(lo) | ((uint32_t) __bfloat16_as_ushort(hi) << 16);
+}
+
+__global__ void __launch_bounds__(kRows) mlp_forward_tc_kernel(MlpDev w, const bf16 *X, long long n, float *y,
+                                                                int *status)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    TcSmem &s = *reinterpret_cast<TcSmem *>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // weights and biases, once per block, in the operand layouts
+    const bf16 *w1t = (const bf16 *) w.w1t, *w2t = (const bf16 *) w.w2t;
+    for (int i = tid; i < kHid * kIn; i += kRows) {
+        const int r = i / kIn, k = i % kIn;
+        *reinterpret_cast<bf16 *>(s.w1 + kmajor_off(r, k, kSbo1)) = w1t[i];
+    }
+    for (int i = tid; i < kHid * kHid; i += kRows) {
+        const int r = i / kHid, k = i % kHid;
+        *reinterpret_cast<bf16 *>(s.w2 + kmajor_off(r, k, kSbo2)) = w2t[i];
+    }
+    for (int i = tid; i < kHid; i += kRows) {
+        s.b1[i] = w.b1[i];
+        s.b2[i] = w.b2[i];
+        s.w3[i] = w.w3[i];
+    }
+    const uint32_t mbar = smem_addr(&s.mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&s.tmem)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = s.tmem;
+    const uint32_t lane_addr = tmem + ((uint32_t) (warp * 32) << 16);  // this warp's 32 TMEM lanes
+    const float b3 = *w.b3;
+    constexpr uint32_t idesc = idesc_bf16(kRows, kHid);
+    const uint32_t sx = smem_addr(s.x), sw1 = smem_addr(s.w1), sh1 = smem_addr(s.h1), sw2 = smem_addr(s.w2);
+    uint32_t phase = 0;
+    bool ok = true;
+    const long long ntiles = (n + kRows - 1) / kRows;
+    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const long long row = tile * kRows + tid;
+        // this thread's feature row, 4 x 16 bytes, zero past n
+        uint4 xr[4] = {};
+        if (row < n) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(X + row * kIn);
+#pragma unroll
+            for (int q = 0; q < 4; q++) xr[q] = src[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) *reinterpret_cast<uint4 *>(s.x + kmajor_off(tid, 8 * q, kSbo1)) = xr[q];
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        fence_after();
+        // layer 1: D1 = X W1 (K = 32: two MMAs of K = 16)
+        if (tid == 0) {
+#pragma unroll
+            for (int ks = 0; ks < kIn / 16; ks++)
+                mma_bf16(tmem, sdesc(sx + ks * 256, 128, kSbo1), sdesc(sw1 + ks * 256, 128, kSbo1), idesc, ks);
+            mma_commit(mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(mbar, phase)) != 0;
+        if (!ok) break;
+        phase ^= 1u;
+        fence_after();
+        // epilogue 1: H1 = bf16(relu(D1 + b1)), row tid, into layer 2's A
+#pragma unroll
+        for (int c0 = 0; c0 < kHid; c0 += 16) {
+            float d[16];
+            tmem_ld16(lane_addr + (uint32_t) c0, d);
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                uint4 v;
+                const int c = c0 + 8 * half;
+                v.x = pack2(fmaxf(d[8 * half + 0] + s.b1[c + 0], 0.0f), fmaxf(d[8 * half + 1] + s.b1[c + 1], 0.0f));
+                v.y = pack2(fmaxf(d[8 * half + 2] + s.b1[c + 2], 0.0f), fmaxf(d[8 * half + 3] + s.b1[c + 3], 0.0f));
+                v.z = pack2(fmaxf(d[8 * half + 4] + s.b1[c + 4], 0.0f), fmaxf(d[8 * half + 5] + s.b1[c + 5], 0.0f));
+                v.w = pack2(fmaxf(d[8 * half + 6] + s.b1[c + 6], 0.0f), fmaxf(d[8 * half + 7] + s.b1[c + 7], 0.0f));
+                *reinterpret_cast<uint4 *>(s.h1 + kmajor_off(tid, c, kSbo2)) = v;
+            }
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        fence_after();
+        // layer 2: D2 = H1 W2 (K = 64: four MMAs), columns 64-127
+        if (tid == 0) {
+#pragma unroll
+            for (int ks = 0; ks < kHid / 16; ks++)
+                mma_bf16(tmem + kHid, sdesc(sh1 + ks * 256, 128, kSbo2), sdesc(sw2 + ks * 256, 128, kSbo2), idesc,
+                         ks);
+            mma_commit(mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(mbar, phase)) != 0;
+        if (!ok) break;
+        phase ^= 1u;
+        fence_after();
+        // epilogue 2: y = relu(D2 + b2) . w3 + b3
+        float acc = 0.0f;
+#pragma unroll
+        for (int c0 = 0; c0 < kHid; c0 += 16) {
+            float d[16];
+            tmem_ld16(lane_addr + (uint32_t) (kHid + c0), d);
+#pragma unroll
+            for (int i = 0; i < 16; i++) acc = fmaf(fmaxf(d[i] + s.b2[c0 + i], 0.0f), s.w3[c0 + i], acc);
+        }
+        if (row < n) y[row] = acc + b3;
+        fence_before();
+        __syncthreads();  // s.x, s.h1 and the accumulators are rewritten by the next tile
+        fence_after();
+    }
+    if (!ok) {
+        if (tid == 0 && status) atomicExch(status, kMlpTcTimeout);
+        mbar_wait(mbar, phase);  // the MMAs in flight, if any (bounded)
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+}  // namespace
+
+cudaError_t mlp_forward_tc(const MlpDev &w, const void *X, long long n, float *y, int *status, cudaStream_t s)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(mlp_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int) kTcSmemBytes);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    if (n <= 0) return cudaSuccess;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long tiles = (n + kRows - 1) / kRows;
+    const long long grid = tiles < 2ll * sms ? tiles : 2ll * sms;
+    mlp_forward_tc_kernel<<<(unsigned) grid, kRows, kTcSmemBytes, s>>>(w, (const bf16 *) X, n, y, status);
+    return cudaGetLastError();
+}
+
+}  // namespace ivr

@@ -103,8 +103,27 @@ def _dev_rows(Xb, T):
     return torch.from_numpy(bits.copy()).cuda(), torch.from_numpy(T).cuda()
 
 
-@pytest.mark.parametrize("n", [1, 300, 1000])
+def _near_bf16_tie(p, x):
+    """Whether one of the row's first-layer values (before its rounding to
+    BF16) lies within FP32 accumulation error of a BF16 rounding tie, so
+    that a different FP32 summation order may round it the other way."""
+    W1, b1 = M.unpack(p)[:2]
+    xe, W1e = M.bf16(x).astype(np.float64), M.bf16(W1).astype(np.float64)
+    v = xe @ W1e + b1
+    mag = np.abs(xe) @ np.abs(W1e) + np.abs(b1)  # bounds every partial sum
+    for j in np.nonzero(v > 0)[0]:
+        ulp = 2.0 ** (np.floor(np.log2(v[j])) - 7)  # one BF16 step at v
+        frac = v[j] / ulp - np.floor(v[j] / ulp)
+        if abs(frac - 0.5) * ulp <= 32 * 2.0 ** -24 * mag[j]:
+            return True
+    return False
+
+
+@pytest.mark.parametrize("n", [1, 300, 1000, 50001])
 def test_forward_matches_oracle(ctx, n):
+    """Inference (the tcgen05 tensor-core kernel: 128-row tiles, a block
+    taking several tiles when there are more than two per SM) against the
+    float64 oracle with the BF16 rounding points."""
     torch = _torch()
     mlp = ctx.mlp(2)
     try:
@@ -120,8 +139,15 @@ def test_forward_matches_oracle(ctx, n):
         mlp.forward(Xd.data_ptr(), n, y.data_ptr())
         yo, _ = M.forward(p_ref, Xb, emulate=True)
         got = _sync_cpu(y)
-        # FP32 accumulation order is the only difference left
-        assert np.max(np.abs(got - yo)) <= 1e-4 * (1 + np.max(np.abs(yo)))
+        # FP32 accumulation order is the only difference left.  On a rare
+        # row it moves a hidden value across a BF16 rounding tie; every row
+        # outside the tight bound must have such a hidden value
+        err = np.abs(got - yo)
+        tol = 1e-4 * (1 + np.max(np.abs(yo)))
+        off = np.nonzero(err > tol)[0]
+        assert len(off) <= max(1, n // 1000), (len(off), err.max())
+        for r in off:
+            assert _near_bf16_tie(p_ref, Xb[r]), (r, err[r])
     finally:
         mlp.free()
 
