@@ -21,6 +21,16 @@ constexpr int kThreads = 128;
 #define IVR_CFG_PAIR 1  // two CONFIG samples per loop iteration
 #endif
 constexpr bool kPair = IVR_CFG_PAIR != 0;
+// The second sample of a PAIR iteration reuses the first's corner-packed
+// cell when both lie in it (for u8 and u16 volumes; IVR_CELL_REUSE=0 turns
+// it off).  Measured on GB300: learned_1024 (u16) +4%; for f32 (16-byte
+// elements, twice the registers per cell) the plain march lost 4% and the
+// skipping march nothing, and keeping the last cell across iterations as
+// well cost more in spills than it saved (sorted_brick_512 -8%).
+#ifndef IVR_CELL_REUSE
+#define IVR_CELL_REUSE 1
+#endif
+template <int DT> __host__ __device__ constexpr bool cell_reuse() { return IVR_CELL_REUSE != 0 && DT != IVR_F32; }
 // Resident blocks per SM each kernel is compiled for.  More warps hide more
 // gather latency; past 8 blocks (64 registers) the compiler spills a little,
 // and measured on GB300 the occupancy still wins: 9 blocks (56 registers)
@@ -274,6 +284,62 @@ __device__ __forceinline__ float sample_cfg(const DevBrick &b, float ux, float u
     return fetch_cfg<DT>(b, cell_cfg(b, ux, uy, uz));
 }
 
+// One voxel cell of a corner-packed copy as loaded: the two elements (slab
+// k and k+1), each holding the cell's four voxels of that slab.  A ray
+// stepping half a voxel takes its next sample in the same cell about half
+// the time; the march keeps the last cell it loaded, with its element
+// offset as the key, and loads again only when the cell changes.  The
+// values are the same voxels, so every sample is bitwise unchanged.
+template <int DT> struct QuadCell;
+template <> struct QuadCell<IVR_U8> { unsigned lo, hi; };
+template <> struct QuadCell<IVR_U16> { uint2 lo, hi; };
+template <> struct QuadCell<IVR_F32> { float4 lo, hi; };
+
+// element offset of cell c in the corner-packed copy (unique per cell)
+__device__ __forceinline__ unsigned quad_key(const DevBrick &b, const CellPos &c)
+{
+    const unsigned qx = (unsigned) b.nx - 1u, qs = qx * ((unsigned) b.ny - 1u);
+    return (unsigned) c.k * qs + (unsigned) c.i * qx + (unsigned) c.j;
+}
+
+template <int DT>
+__device__ __forceinline__ QuadCell<DT> quad_load(const DevBrick &b, unsigned key)
+{
+    using E = decltype(QuadCell<DT>::lo);
+    const unsigned qs = ((unsigned) b.nx - 1u) * ((unsigned) b.ny - 1u);
+    const E *e = reinterpret_cast<const E *>(b.quad) + key;
+    QuadCell<DT> q;
+    q.lo = __ldg(e);
+    q.hi = __ldg(e + qs);
+    return q;
+}
+
+// fetch_cfg's corner-packed interpolation on a loaded cell
+template <int DT>
+__device__ __forceinline__ float quad_interp(const QuadCell<DT> &q, const CellPos &c)
+{
+    float c00, c10, c01, c11;
+    if constexpr (DT == IVR_U8) {
+        c00 = lerp23(off23(q.lo, kU8Lane0), off23(q.lo, kU8Lane1), c.fx);
+        c10 = lerp23(off23(q.lo, kU8Lane2), off23(q.lo, kU8Lane3), c.fx);
+        c01 = lerp23(off23(q.hi, kU8Lane0), off23(q.hi, kU8Lane1), c.fx);
+        c11 = lerp23(off23(q.hi, kU8Lane2), off23(q.hi, kU8Lane3), c.fx);
+    } else if constexpr (DT == IVR_U16) {
+        c00 = lerp23(off23(q.lo.x, kU16Half0), off23(q.lo.x, kU16Half1), c.fx);
+        c10 = lerp23(off23(q.lo.y, kU16Half0), off23(q.lo.y, kU16Half1), c.fx);
+        c01 = lerp23(off23(q.hi.x, kU16Half0), off23(q.hi.x, kU16Half1), c.fx);
+        c11 = lerp23(off23(q.hi.y, kU16Half0), off23(q.hi.y, kU16Half1), c.fx);
+    } else {
+        c00 = lerpf(q.lo.x, q.lo.y, c.fx);
+        c10 = lerpf(q.lo.z, q.lo.w, c.fx);
+        c01 = lerpf(q.hi.x, q.hi.y, c.fx);
+        c11 = lerpf(q.hi.z, q.hi.w, c.fx);
+    }
+    const float c0 = lerpf(c00, c10, c.fy);
+    const float c1 = lerpf(c01, c11, c.fy);
+    return lerpf(c0, c1, c.fz);
+}
+
 // A ray's CONFIG lattice in a brick's voxel coordinates: lattice index i
 // samples u_i = fmaf(i, s, base) per axis, with s = (d * ic) * dt and
 // base = fmaf(d * ic, t0, (o - bmin) * ic) -- the point o + t_i d, t_i =
@@ -524,8 +590,19 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
         if (PAIR && !CENSUS) {
             const int lim = SKIP ? min(i1, icheck) : i1;
             const float f1 = fi + 1.0f;  // (float) (i + 1): i < 2^24
-            const float s0 = fetch_cfg<DT>(b, c0);
-            const float s1 = sample_cfg<DT>(b, fmaf(f1, L.sx, L.bx), fmaf(f1, L.sy, L.by), fmaf(f1, L.sz, L.bz));
+            float s0, s1;
+            if (cell_reuse<DT>() && b.quad) {
+                const CellPos c1 = cell_cfg(b, fmaf(f1, L.sx, L.bx), fmaf(f1, L.sy, L.by), fmaf(f1, L.sz, L.bz));
+                const unsigned k0 = quad_key(b, c0), k1 = quad_key(b, c1);
+                const QuadCell<DT> q0 = quad_load<DT>(b, k0);
+                QuadCell<DT> q1 = q0;
+                if (k1 != k0) q1 = quad_load<DT>(b, k1);
+                s0 = quad_interp<DT>(q0, c0);
+                s1 = quad_interp<DT>(q1, c1);
+            } else {
+                s0 = fetch_cfg<DT>(b, c0);
+                s1 = sample_cfg<DT>(b, fmaf(f1, L.sx, L.bx), fmaf(f1, L.sy, L.by), fmaf(f1, L.sz, L.bz));
+            }
             const float4 e0 = lut_at(f, (int) (s0 * f.lut_scale) - f.lut_off);
             const float4 e1 = lut_at(f, (int) (s1 * f.lut_scale) - f.lut_off);
             float wgt = (1.0f - acc.w) * (e0.w * opac);
@@ -1043,8 +1120,21 @@ __global__ void __launch_bounds__(kThreads, kCfgBlocksPerSm) sample_peak_kernel(
     const float loy = 1.0f, hiy = sy - 1.0f;
     const float loz = 1.0f, hiz = sz - 1.0f;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    QuadCell<DT> qlast{};
+    unsigned qkey = 0;
     for (int i = 0; i < steps; i++) {
-        const float s = sample_layout<DT, LAYOUT>(b, tex, x, y, z);
+        float s;
+        if (LAYOUT == IVR_SAMPLER_QUADS && cell_reuse<DT>()) {
+            // the march's sampler: samples taken in pairs, the second
+            // reusing the first's cell when both lie in it
+            const CellPos c = cell_cfg(b, x, y, z);
+            const unsigned k = quad_key(b, c);
+            if (!(i & 1) || k != qkey) qlast = quad_load<DT>(b, k);
+            qkey = k;
+            s = quad_interp<DT>(qlast, c);
+        } else {
+            s = sample_layout<DT, LAYOUT>(b, tex, x, y, z);
+        }
         const float4 e = lut_at(f, (int) (s * f.lut_scale) - f.lut_off);
         const float wgt = (1.0f - acc.w) * (e.w * f.alpha);
         acc.x = fmaf(wgt, e.x, acc.x);
