@@ -417,6 +417,13 @@ int ivr_volume_set_mlp(ivr_volume *vol, ivr_mlp *mlp, float margin, int certify)
  * stats[0] cells, [1] exactly transparent cells, [2] cells the predictor
  * called transparent, [3] false skips among them. */
 int ivr_volume_learned_stats(ivr_volume *vol, unsigned long long *stats);
+/* The skipping grid that frames of the given skip mode (IVR_SKIP_GRID or
+ * IVR_SKIP_LEARNED) use for tf, built if needed, for one brick: per
+ * macrocell (x fastest, dims[0] x dims[1] x dims[2] cells) 0 where a sample
+ * can be opaque, else r >= 1 = every cell within r - 1 cells (Chebyshev) is
+ * transparent, capped (at 8 unless built otherwise).  Copies it into host memory cells (capacity n
+ * bytes) and waits; with cells = NULL only dims is filled. */
+int ivr_volume_skip_grid(ivr_volume *vol, ivr_tf *tf, int skip, int brick, uint8_t *cells, long long n, int *dims);
 /* The judge's totals over the view's learned-skip frames (waits for them). */
 int ivr_view_judge_stats(ivr_view *view, ivr_judge_stats *stats);
 

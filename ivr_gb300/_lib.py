@@ -176,6 +176,7 @@ SIGNATURES = {
     "ivr_volume_set_mlp": (_I, [_P, _P, _F, _I]),
     "ivr_view_judge_stats": (_I, [_P, ctypes.POINTER(JudgeStats)]),
     "ivr_volume_learned_stats": (_I, [_P, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "ivr_volume_skip_grid": (_I, [_P, _P, _I, _I, _P, ctypes.c_longlong, _PI]),
     "ivr_sample_peak": (_I, [_P, _I, ctypes.POINTER(ctypes.c_double), _P]),
     "ivr_sample_peak_layout": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _P]),
     "ivr_composite": (_I, [_P, _P, _P, _I, _I, _I, _P]),

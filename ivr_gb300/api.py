@@ -223,6 +223,18 @@ class Volume:
         self.ctx.check(self.ctx.lib.ivr_volume_learned_stats(self.h, st))
         return {"cells": st[0], "exact_transparent": st[1], "learned_transparent": st[2], "false_skips": st[3]}
 
+    def skip_grid(self, tf, skip=None, brick=0):
+        """The skipping grid frames of `skip` (SKIP_GRID or SKIP_LEARNED) use
+        for tf, one brick's macrocells as uint8 [z][y][x]: 0 where a sample
+        can be opaque, r >= 1 where every cell within r - 1 is transparent."""
+        skip = SKIP_GRID if skip is None else skip
+        dims = (ctypes.c_int * 3)()
+        lib = self.ctx.lib
+        self.ctx.check(lib.ivr_volume_skip_grid(self.h, tf.h, skip, brick, None, 0, dims))
+        out = np.zeros((dims[2], dims[1], dims[0]), np.uint8)
+        self.ctx.check(lib.ivr_volume_skip_grid(self.h, tf.h, skip, brick, out.ctypes.data, out.size, dims))
+        return out
+
     def free(self):
         if self.h:
             self.ctx.lib.ivr_volume_free(self.h)

@@ -778,6 +778,32 @@ int ivr_volume_free(ivr_volume *v)
     return IVR_OK;
 }
 
+int ivr_volume_skip_grid(ivr_volume *v, ivr_tf *tf, int skip, int brick, uint8_t *cells, long long n, int *dims)
+{
+    if (!v) return IVR_ERR_INVALID;
+    ivr_ctx *c = v->ctx;
+    if (!tf) return fail(c, IVR_ERR_INVALID, "null transfer function");
+    if (skip != IVR_SKIP_GRID && skip != IVR_SKIP_LEARNED)
+        return fail(c, IVR_ERR_INVALID, "skip %d: the grids are IVR_SKIP_GRID's and IVR_SKIP_LEARNED's", skip);
+    if (brick < 0 || brick >= (int) v->bricks.size())
+        return fail(c, IVR_ERR_INVALID, "brick %d of %d", brick, (int) v->bricks.size());
+    const HostBrick &b = v->bricks[brick];
+    if (dims) {
+        dims[0] = b.mcx;
+        dims[1] = b.mcy;
+        dims[2] = b.mcz;
+    }
+    if (!cells) return IVR_OK;
+    const long long ncell = (long long) mc_cells(b);
+    if (n < ncell) return fail(c, IVR_ERR_INVALID, "%lld bytes for a grid of %lld cells", n, ncell);
+    ivr_volume::TfGrid *g = nullptr;
+    int rc = tf_grid(v, tf, false, skip == IVR_SKIP_LEARNED, 0, c->grid_clock + 1, &g);
+    if (rc) return rc;
+    CK(c, cudaEventSynchronize(g->built));
+    CK(c, cudaMemcpy(cells, g->dist[brick], (size_t) ncell, cudaMemcpyDeviceToHost));
+    return IVR_OK;
+}
+
 int ivr_bricks_setup(ivr_volume *v, int py, int px, int pz, int overlap)
 {
     if (!v) return IVR_ERR_INVALID;

@@ -194,8 +194,8 @@ long long judge_scratch_bytes(const FrameDesc &f);
 // the CONFIG tile order of f, costliest first, into perm (ntiles ints) with
 // key (ntiles bytes) and counts (128 ints) as scratch
 cudaError_t launch_tile_order(const FrameDesc &f, uint8_t *key, int *counts, int *perm, cudaStream_t s);
-// transparent-radius relaxation of a flag grid (kDistCap or 0 per cell)
-cudaError_t launch_dist_relax(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s);
+// the capped distance transform of a flag grid (kDistCap or 0 per cell), in place
+cudaError_t launch_dist_transform(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s);
 // per macrocell 255 sqrt(mean LUT opacity over its value range) (DevBrick::opac)
 cudaError_t launch_cell_opacity(const float *mc, int mcx, int mcy, int mcz, const double *aprefix, int lut_n,
                                 int lut_off, float lut_scale, uint8_t *opac, cudaStream_t s);

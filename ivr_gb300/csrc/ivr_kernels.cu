@@ -177,29 +177,76 @@ __global__ void cell_opacity_kernel(const float *mc, int ncell, const double *ap
     }
 }
 
-// One relaxation step of the Chebyshev distance (in cells) from each
-// transparent cell to the nearest opaque one: d = min(cap, 1 + min over the
-// 26 neighbours), 0 for opaque cells; cells outside the grid count as
-// transparent (a ray there has left the brick).  After kDistCap steps d is
-// the exact distance where that is below the cap, and the cap elsewhere, so
-// every cell within d-1 of a cell with d >= 1 is transparent.  Updating in
-// place only propagates smaller values sooner, which keeps that true.
-__global__ void dist_relax_kernel(uint8_t *dist, int mcx, int mcy, int mcz)
+// The Chebyshev distance (in cells) from each transparent cell to the
+// nearest opaque one, capped: d = min(cap, max(|dx|, |dy|, |dz|) to the
+// nearest cell with flag 0), 0 for opaque cells; cells outside the grid are
+// not opaque (a ray there has left the brick).  Every cell within d-1 of a
+// cell with d >= 1 is then transparent.  The L-infinity distance separates
+// by axis: with g0 = 0 (opaque) or cap (transparent) and, along each axis
+// in turn, g(p) = min over |k| <= cap of max(|k|, g(p + k)), three passes
+// give the distance exactly (a minimum over the cells of the window of the
+// largest per-axis offset; anything farther than the cap is the cap).
+//
+// One pass over the lines along `axis` (0 = x, 1 = y, 2 = z), in place: a
+// block takes 32 neighbouring lines whole (neighbours along x for the y and
+// z passes, along y for the x pass), so that its loads and stores coalesce,
+// stages them in shared memory and writes them back once all are read.
+constexpr int kDistLines = 32;
+__global__ void dist_axis_kernel(uint8_t *dist, int mcx, int mcy, int mcz, int axis)
 {
-    const int ncell = mcx * mcy * mcz;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
-        if (dist[c] == 0) continue;
-        const int x = c % mcx, y = (c / mcx) % mcy, z = c / (mcx * mcy);
-        int m = kDistCap;
-        for (int dz = -1; dz <= 1; dz++)
-            for (int dy = -1; dy <= 1; dy++)
-                for (int dx = -1; dx <= 1; dx++) {
-                    const int xx = x + dx, yy = y + dy, zz = z + dz;
-                    if ((dx | dy | dz) == 0 || xx < 0 || yy < 0 || zz < 0 || xx >= mcx || yy >= mcy || zz >= mcz)
-                        continue;
-                    m = min(m, (int) dist[((long long) zz * mcy + yy) * mcx + xx]);
-                }
-        dist[c] = (uint8_t) min(kDistCap, m + 1);
+    extern __shared__ uint8_t tile[];  // [L][kDistLines + 1]
+    constexpr int P = kDistLines + 1;
+    const int L = axis == 0 ? mcx : axis == 1 ? mcy : mcz;
+    const long long slab = (long long) mcx * mcy;
+    const long long stride = axis == 0 ? 1 : axis == 1 ? mcx : slab;
+    // this block's group of lines: the first line's base and the distance
+    // between neighbouring lines; nl lines are in the grid
+    const int across = axis == 0 ? mcy : mcx;  // lines of a group run along this dimension
+    const int groups_across = (across + kDistLines - 1) / kDistLines;
+    const long long g = blockIdx.x;
+    const int outer = (int) (g / groups_across), first = (int) (g % groups_across) * kDistLines;
+    const int nl = min(kDistLines, across - first);
+    long long base;
+    long long step;
+    if (axis == 0) {  // rows (y, z): outer = z, lines along y
+        base = ((long long) outer * mcy + first) * mcx;
+        step = mcx;
+    } else if (axis == 1) {  // columns (x, z): outer = z, lines along x
+        base = (long long) outer * slab + first;
+        step = 1;
+    } else {  // pillars (x, y): outer = y, lines along x
+        base = (long long) outer * mcx + first;
+        step = 1;
+    }
+    const int n = L * nl;
+    // element e of the group: line l, position p (the x pass walks a row's
+    // bytes with neighbouring threads, the others neighbouring lines); four
+    // loads in flight per thread before their stores
+    constexpr int U = 4;
+    for (int e0 = threadIdx.x; e0 < n; e0 += U * blockDim.x) {
+        uint8_t v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int e = e0 + u * blockDim.x;
+            const int l = axis == 0 ? e / L : e % nl, p = axis == 0 ? e % L : e / nl;
+            v[u] = e < n ? dist[base + l * step + p * stride] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int e = e0 + u * blockDim.x;
+            const int l = axis == 0 ? e / L : e % nl, p = axis == 0 ? e % L : e / nl;
+            if (e < n) tile[p * P + l] = v[u];
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int l = axis == 0 ? e / L : e % nl, p = axis == 0 ? e % L : e / nl;
+        int m = tile[p * P + l];
+        for (int k = 1; k < m; k++) {  // only offsets below the current minimum can lower it
+            if (p - k >= 0) m = min(m, max(k, (int) tile[(p - k) * P + l]));
+            if (p + k < L) m = min(m, max(k, (int) tile[(p + k) * P + l]));
+        }
+        dist[base + l * step + p * stride] = (uint8_t) m;
     }
 }
 
@@ -390,7 +437,7 @@ cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const
 {
     const int ncell = mcx * mcy * mcz;
     empty_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mc, ncell, nzprefix, lut_n, lut_off, lut_scale, empty);
-    return launch_dist_relax(empty, mcx, mcy, mcz, s);
+    return launch_dist_transform(empty, mcx, mcy, mcz, s);
 }
 
 cudaError_t launch_cell_opacity(const float *mc, int mcx, int mcy, int mcz, const double *aprefix, int lut_n,
@@ -401,11 +448,19 @@ cudaError_t launch_cell_opacity(const float *mc, int mcx, int mcy, int mcz, cons
     return cudaGetLastError();
 }
 
-cudaError_t launch_dist_relax(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s)
+cudaError_t launch_dist_transform(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s)
 {
-    const int ncell = mcx * mcy * mcz;
-    for (int it = 0; it < kDistCap; it++)
-        dist_relax_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(dist, mcx, mcy, mcz);
+    if (mcx <= 0 || mcy <= 0 || mcz <= 0) return cudaSuccess;
+    const int dims[3] = {mcx, mcy, mcz};
+    for (int axis = 0; axis < 3; axis++) {
+        const int L = dims[axis];
+        if (L == 1) continue;  // a line of one cell keeps its flag
+        const size_t smem = (size_t) L * (kDistLines + 1);
+        if (smem > 48 * 1024) return cudaErrorInvalidValue;  // lines of more than 1489 cells
+        const int across = axis == 0 ? mcy : mcx, outer = axis == 2 ? mcy : mcz;
+        const long long groups = (long long) outer * ((across + kDistLines - 1) / kDistLines);
+        dist_axis_kernel<<<(unsigned) groups, 256, smem, s>>>(dist, mcx, mcy, mcz, axis);
+    }
     return cudaGetLastError();
 }
 

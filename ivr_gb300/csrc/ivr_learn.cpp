@@ -32,15 +32,11 @@ struct ivr_mlp {
     int *d_idx = nullptr;
     float *d_loss = nullptr;
     long long loss_cap = 0;
-    // inference scratch of the learned fields (one brick at a time)
-    uint16_t *d_xs = nullptr;
-    float *d_ys = nullptr;
-    long long scap = 0;
-    float *d_knots = nullptr;
+    float *d_knots = nullptr;  // the knots of the TF whose learned grid is being built
     int *d_key = nullptr;
     int *d_status = nullptr;  // inference status word (kMlpTcTimeout)
     unsigned long long *d_counts = nullptr;
-    cudaEvent_t scratch_ev = nullptr;  // after the last use of the scratch
+    cudaEvent_t scratch_ev = nullptr;  // after the last use of d_knots
 };
 
 namespace {
@@ -162,9 +158,10 @@ void ivr::learned_release(ivr_volume *v)
     v->cell_hist.clear();
 }
 
-// Per brick: features -> forward -> y + margin <= 0 -> distance relaxation.
-// The predictor's scratch is shared by every volume it is attached to, so
-// builds are ordered on the device through its event.
+// Per brick: one launch for the features, the network and the certified
+// flags, then the distance transform.  The predictor's knot scratch is
+// shared by every volume it is attached to, so builds are ordered on the
+// device through its event.
 int ivr::learned_fields(ivr_volume *v, const ivr_tf *tf, const std::vector<uint8_t *> &dist, cudaStream_t s)
 {
     ivr_mlp *m = v->mlp;
@@ -173,30 +170,28 @@ int ivr::learned_fields(ivr_volume *v, const ivr_tf *tf, const std::vector<uint8
     if (rc) return rc;
     rc = ensure_cell_hist(v, s);
     if (rc) return rc;
-    long long most = 0;
-    for (const auto &b : v->bricks) most = std::max(most, (long long) mc_cells(b));
-    if (most > m->scap) {
-        CK(c, cudaEventSynchronize(m->scratch_ev));
-        long long cap = m->scap;
-        rc = grow(c, (void **) &m->d_xs, &cap, most, kMlpIn * kBf16Bytes, 0);
-        if (rc) return rc;
-        cap = m->scap;
-        rc = grow(c, (void **) &m->d_ys, &cap, most, sizeof(float), 0);
-        if (rc) return rc;
-        m->scap = cap;
-    }
     CK(c, cudaStreamWaitEvent(s, m->scratch_ev, 0));
     CK(c, mlp_tf_knots(tf->d_lut, tf->n, tf->off, tf->scale, v->vmin, v->vmax, m->d_knots, s));
     const MlpDev w = dev_of(m);
     for (size_t k = 0; k < v->bricks.size(); k++) {
         const HostBrick &b = v->bricks[k];
-        const int ncell = (int) mc_cells(b);
-        CK(c, mlp_cell_features(b.mc_minmax, v->cell_hist[k], ncell, v->vmin, v->vmax, m->d_knots, tf->d_lut, tf->n,
-                                tf->off, tf->scale, m->d_xs, nullptr, s));
-        CK(c, mlp_forward(w, m->d_xs, ncell, m->d_ys, s));
-        CK(c, mlp_learned_flags(m->d_ys, ncell, v->mlp_margin, dist[k], b.mc_minmax, tf->d_nzprefix, tf->n, tf->off,
-                                tf->scale, v->mlp_certify ? 1 : 0, v->d_lstats, s));
-        CK(c, launch_dist_relax(dist[k], b.mcx, b.mcy, b.mcz, s));
+        MlpGridArgs g{};
+        g.mc = b.mc_minmax;
+        g.hist = v->cell_hist[k];
+        g.knots = m->d_knots;
+        g.ncell = (int) mc_cells(b);
+        g.vmin = v->vmin;
+        g.vmax = v->vmax;
+        g.margin = v->mlp_margin;
+        g.nzprefix = tf->d_nzprefix;
+        g.lut_n = tf->n;
+        g.lut_off = tf->off;
+        g.lut_scale = tf->scale;
+        g.certify = v->mlp_certify ? 1 : 0;
+        g.dist = dist[k];
+        g.stats = v->d_lstats;
+        CK(c, mlp_learned_grid_tc(w, g, s));
+        CK(c, launch_dist_transform(dist[k], b.mcx, b.mcy, b.mcz, s));
     }
     CK(c, cudaEventRecord(m->scratch_ev, s));
     return IVR_OK;
@@ -221,8 +216,6 @@ int ivr_mlp_free(ivr_mlp *m)
     dev_free(c, m->d_Y, (size_t) m->cap * sizeof(float));
     dev_free(c, m->d_idx, (size_t) m->cap * sizeof(int));
     dev_free(c, m->d_loss, (size_t) m->loss_cap * sizeof(float));
-    dev_free(c, m->d_xs, (size_t) m->scap * kMlpIn * kBf16Bytes);
-    dev_free(c, m->d_ys, (size_t) m->scap * sizeof(float));
     dev_free(c, m->d_knots, kMlpKnots * sizeof(float));
     dev_free(c, m->d_key, sizeof(int));
     dev_free(c, m->d_status, sizeof(int));

@@ -31,6 +31,14 @@ constexpr bool kPair = IVR_CFG_PAIR != 0;
 #define IVR_CELL_REUSE 1
 #endif
 template <int DT> __host__ __device__ constexpr bool cell_reuse() { return IVR_CELL_REUSE != 0 && DT != IVR_F32; }
+// Likewise its LUT entry when both samples index the same one (every dtype;
+// IVR_LUT_REUSE=0 turns it off): +1-2% on learned_1024 and the plain march.
+// A copy of the LUT in each block's shared memory instead of reads through
+// L1 was 2-4% slower.
+#ifndef IVR_LUT_REUSE
+#define IVR_LUT_REUSE 1
+#endif
+constexpr bool kLutReuse = IVR_LUT_REUSE != 0;
 // Resident blocks per SM each kernel is compiled for.  More warps hide more
 // gather latency; past 8 blocks (64 registers) the compiler spills a little,
 // and measured on GB300 the occupancy still wins: 9 blocks (56 registers)
@@ -603,8 +611,10 @@ __device__ void march_cfg(const FrameDesc &f, const DevBrick &b, const uint8_t *
                 s0 = fetch_cfg<DT>(b, c0);
                 s1 = sample_cfg<DT>(b, fmaf(f1, L.sx, L.bx), fmaf(f1, L.sy, L.by), fmaf(f1, L.sz, L.bz));
             }
-            const float4 e0 = lut_at(f, (int) (s0 * f.lut_scale) - f.lut_off);
-            const float4 e1 = lut_at(f, (int) (s1 * f.lut_scale) - f.lut_off);
+            const int x0 = (int) (s0 * f.lut_scale) - f.lut_off, x1 = (int) (s1 * f.lut_scale) - f.lut_off;
+            const float4 e0 = lut_at(f, x0);
+            float4 e1 = e0;
+            if (!kLutReuse || x1 != x0) e1 = lut_at(f, x1);  // the same entry: no second load
             float wgt = (1.0f - acc.w) * (e0.w * opac);
             acc.x = fmaf(wgt, e0.x, acc.x);
             acc.y = fmaf(wgt, e0.y, acc.y);

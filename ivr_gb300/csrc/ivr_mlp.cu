@@ -419,42 +419,6 @@ __global__ void tf_knots_kernel(const float4 *lut, int lut_n, int lut_off, float
     if (lane == 0) knots[k] = m;
 }
 
-// Learned transparency (y + margin <= 0).  With certify the exact
-// empty-cell test is applied too: a cell called transparent whose LUT index
-// range holds a nonzero opacity (a false skip) is kept opaque.  stats (4
-// counters, nullable) accumulates cells, exactly transparent cells, cells
-// called transparent and false skips.
-__global__ void learned_flags_kernel(const float *y, int ncell, float margin, uint8_t *dist, const float *mc,
-                                     const int *nzprefix, int lut_n, int lut_off, float lut_scale, int certify,
-                                     unsigned long long *stats)
-{
-    unsigned n = 0, nexact = 0, nlearned = 0, nfalse = 0;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
-        const bool learned = y[c] + margin <= 0.0f;
-        const int lo = min(max((int) (mc[2 * c] * lut_scale) - 1 - lut_off, 0), lut_n - 1);
-        const int hi = min(max((int) (mc[2 * c + 1] * lut_scale) + 1 - lut_off, 0), lut_n - 1);
-        const bool exact = (nzprefix[hi + 1] - nzprefix[lo]) == 0;
-        dist[c] = (learned && (exact || !certify)) ? (uint8_t) kDistCap : 0;
-        n++;
-        nexact += exact;
-        nlearned += learned;
-        nfalse += learned && !exact;
-    }
-    if (!stats) return;
-    for (int o = 16; o > 0; o >>= 1) {
-        n += __shfl_xor_sync(0xffffffffu, n, o);
-        nexact += __shfl_xor_sync(0xffffffffu, nexact, o);
-        nlearned += __shfl_xor_sync(0xffffffffu, nlearned, o);
-        nfalse += __shfl_xor_sync(0xffffffffu, nfalse, o);
-    }
-    if ((threadIdx.x & 31) == 0 && n) {
-        atomicAdd(stats, (unsigned long long) n);
-        atomicAdd(stats + 1, (unsigned long long) nexact);
-        atomicAdd(stats + 2, (unsigned long long) nlearned);
-        if (nfalse) atomicAdd(stats + 3, (unsigned long long) nfalse);
-    }
-}
-
 // order-preserving float <-> int keys for atomicMax
 __device__ __forceinline__ int float_key(float f)
 {
@@ -556,15 +520,6 @@ cudaError_t mlp_tf_knots(const float4 *lut, int lut_n, int lut_off, float lut_sc
                          float *knots, cudaStream_t s)
 {
     tf_knots_kernel<<<1, 32 * kMlpKnots, 0, s>>>(lut, lut_n, lut_off, lut_scale, vmin, vmax, knots);
-    return cudaGetLastError();
-}
-
-cudaError_t mlp_learned_flags(const float *y, int ncell, float margin, uint8_t *dist, const float *mc,
-                              const int *nzprefix, int lut_n, int lut_off, float lut_scale, int certify,
-                              unsigned long long *stats, cudaStream_t s)
-{
-    learned_flags_kernel<<<grid_of(ncell, 256), 256, 0, s>>>(y, ncell, margin, dist, mc, nzprefix, lut_n, lut_off,
-                                                             lut_scale, certify, stats);
     return cudaGetLastError();
 }
 

@@ -54,13 +54,27 @@ cudaError_t mlp_cell_features(const float *mc, const float *hist, int ncell, flo
                               void *X, float *targets, cudaStream_t s);
 cudaError_t mlp_tf_knots(const float4 *lut, int lut_n, int lut_off, float lut_scale, float vmin, float vmax,
                          float *knots, cudaStream_t s);
-// transparent flags (kDistCap / 0) of y + margin <= 0; with certify a cell
-// the exact test (mc, nzprefix, LUT index rule) finds opaque stays opaque.
-// stats (nullable): += cells, exactly transparent, called transparent,
-// false skips
-cudaError_t mlp_learned_flags(const float *y, int ncell, float margin, uint8_t *dist, const float *mc,
-                              const int *nzprefix, int lut_n, int lut_off, float lut_scale, int certify,
-                              unsigned long long *stats, cudaStream_t s);
+// One brick's learned grid for one TF, in one launch: each cell's features
+// (as mlp_cell_features writes them), the network (as mlp_forward runs it)
+// and the transparent flag (kDistCap / 0) of y + margin <= 0; with certify
+// a cell the exact test (mc, nzprefix, LUT index rule) finds opaque stays
+// opaque.  stats (nullable): += cells, exactly transparent, called
+// transparent, false skips.  Cells a block could not finish (a tensor-core
+// wait ran out: *w.status) are left opaque.
+struct MlpGridArgs {
+    const float *mc;        // per cell: min, max
+    const float *hist;      // per cell: 8 bins
+    const float *knots;     // the TF's 16 knots
+    int ncell;
+    float vmin, vmax, margin;
+    const int *nzprefix;    // count of nonzero-opacity LUT entries below each index
+    int lut_n, lut_off;
+    float lut_scale;
+    int certify;
+    uint8_t *dist;          // out: kDistCap or 0 per cell
+    unsigned long long *stats;
+};
+cudaError_t mlp_learned_grid_tc(const MlpDev &w, const MlpGridArgs &g, cudaStream_t s);
 // *key (initialised to the key of -FLT_MAX) = key of the largest -y over
 // rows with T > 0; counts[0] += rows with T <= 0, counts[1] += those with
 // y + margin <= 0

@@ -122,8 +122,11 @@ __device__ __forceinline__ uint32_t pack2(float a, float b)
     return (uint32_t) __bfloat16_as_ushort(lo) | ((uint32_t) __bfloat16_as_ushort(hi) << 16);
 }
 
-__global__ void __launch_bounds__(kRows) mlp_forward_tc_kernel(MlpDev w, const bf16 *X, long long n, float *y,
-                                                                int *status)
+// GRID: the rows are the cells of g (features built here, flags written
+// instead of y); otherwise rows of X in, y out.
+template <bool GRID>
+__global__ void __launch_bounds__(kRows) mlp_tc_kernel(MlpDev w, const bf16 *X, long long n, float *y, int *status,
+                                                        MlpGridArgs g)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     TcSmem &s = *reinterpret_cast<TcSmem *>(smem_raw);
@@ -165,14 +168,39 @@ __global__ void __launch_bounds__(kRows) mlp_forward_tc_kernel(MlpDev w, const b
     uint32_t phase = 0;
     bool ok = true;
     const long long ntiles = (n + kRows - 1) / kRows;
-    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    // GRID: the TF's knots (the same for every cell) and the cell counts
+    float knot[kMlpKnots];
+    if (GRID)
+#pragma unroll
+        for (int k = 0; k < kMlpKnots; k++) knot[k] = g.knots[k];
+    const float inv = g.vmax > g.vmin ? 1.0f / (g.vmax - g.vmin) : 0.0f;
+    unsigned ncells = 0, nexact = 0, nlearned = 0, nfalse = 0;
+    long long tile = blockIdx.x;
+    for (; tile < ntiles && ok; tile += gridDim.x) {
         const long long row = tile * kRows + tid;
         // this thread's feature row, 4 x 16 bytes, zero past n
         uint4 xr[4] = {};
+        float lo = 0.0f, hi = 0.0f;
         if (row < n) {
-            const uint4 *src = reinterpret_cast<const uint4 *>(X + row * kIn);
+            if (GRID) {
+                // the row mlp_cell_features writes: min and max normalised, 8 bins,
+                // 16 knots, zero padding
+                lo = g.mc[2 * row];
+                hi = g.mc[2 * row + 1];
+                const float4 h0 = reinterpret_cast<const float4 *>(g.hist + row * 8)[0];
+                const float4 h1 = reinterpret_cast<const float4 *>(g.hist + row * 8)[1];
+                xr[0] = make_uint4(pack2((lo - g.vmin) * inv, (hi - g.vmin) * inv), pack2(h0.x, h0.y),
+                                   pack2(h0.z, h0.w), pack2(h1.x, h1.y));
+                xr[1] = make_uint4(pack2(h1.z, h1.w), pack2(knot[0], knot[1]), pack2(knot[2], knot[3]),
+                                   pack2(knot[4], knot[5]));
+                xr[2] = make_uint4(pack2(knot[6], knot[7]), pack2(knot[8], knot[9]), pack2(knot[10], knot[11]),
+                                   pack2(knot[12], knot[13]));
+                xr[3] = make_uint4(pack2(knot[14], knot[15]), 0u, 0u, 0u);
+            } else {
+                const uint4 *src = reinterpret_cast<const uint4 *>(X + row * kIn);
 #pragma unroll
-            for (int q = 0; q < 4; q++) xr[q] = src[q];
+                for (int q = 0; q < 4; q++) xr[q] = src[q];
+            }
         }
 #pragma unroll
         for (int q = 0; q < 4; q++) *reinterpret_cast<uint4 *>(s.x + kmajor_off(tid, 8 * q, kSbo1)) = xr[q];
@@ -232,7 +260,23 @@ __global__ void __launch_bounds__(kRows) mlp_forward_tc_kernel(MlpDev w, const b
 #pragma unroll
             for (int i = 0; i < 16; i++) acc = fmaf(fmaxf(d[i] + s.b2[c0 + i], 0.0f), s.w3[c0 + i], acc);
         }
-        if (row < n) y[row] = acc + b3;
+        if (row < n) {
+            const float yv = acc + b3;
+            if (GRID) {
+                // learned transparency, certified by the exact empty-cell test
+                const bool learned = yv + g.margin <= 0.0f;
+                const int a = min(max((int) (lo * g.lut_scale) - 1 - g.lut_off, 0), g.lut_n - 1);
+                const int b = min(max((int) (hi * g.lut_scale) + 1 - g.lut_off, 0), g.lut_n - 1);
+                const bool exact = (g.nzprefix[b + 1] - g.nzprefix[a]) == 0;
+                g.dist[row] = (learned && (exact || !g.certify)) ? (uint8_t) kDistCap : 0;
+                ncells++;
+                nexact += exact;
+                nlearned += learned;
+                nfalse += learned && !exact;
+            } else {
+                y[row] = yv;
+            }
+        }
         fence_before();
         __syncthreads();  // s.x, s.h1 and the accumulators are rewritten by the next tile
         fence_after();
@@ -240,6 +284,25 @@ __global__ void __launch_bounds__(kRows) mlp_forward_tc_kernel(MlpDev w, const b
     if (!ok) {
         if (tid == 0 && status) atomicExch(status, kMlpTcTimeout);
         mbar_wait(mbar, phase);  // the MMAs in flight, if any (bounded)
+        if (GRID)  // the cells this block did not finish stay opaque
+            for (; tile < ntiles; tile += gridDim.x) {
+                const long long row = tile * kRows + tid;
+                if (row < n) g.dist[row] = 0;
+            }
+    }
+    if (GRID && g.stats) {
+        for (int o = 16; o > 0; o >>= 1) {
+            ncells += __shfl_xor_sync(0xffffffffu, ncells, o);
+            nexact += __shfl_xor_sync(0xffffffffu, nexact, o);
+            nlearned += __shfl_xor_sync(0xffffffffu, nlearned, o);
+            nfalse += __shfl_xor_sync(0xffffffffu, nfalse, o);
+        }
+        if ((tid & 31) == 0 && ncells) {
+            atomicAdd(g.stats, (unsigned long long) ncells);
+            atomicAdd(g.stats + 1, (unsigned long long) nexact);
+            atomicAdd(g.stats + 2, (unsigned long long) nlearned);
+            if (nfalse) atomicAdd(g.stats + 3, (unsigned long long) nfalse);
+        }
     }
     fence_before();
     __syncthreads();
@@ -249,11 +312,14 @@ __global__ void __launch_bounds__(kRows) mlp_forward_tc_kernel(MlpDev w, const b
 
 }  // namespace
 
-cudaError_t mlp_forward_tc(const MlpDev &w, const void *X, long long n, float *y, int *status, cudaStream_t s)
+namespace {
+
+template <bool GRID>
+cudaError_t launch_tc(const MlpDev &w, const void *X, long long n, float *y, const MlpGridArgs &g, cudaStream_t s)
 {
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(mlp_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel<GRID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int) kTcSmemBytes);
         if (e != cudaSuccess) return e;
         attr = true;
@@ -264,8 +330,22 @@ cudaError_t mlp_forward_tc(const MlpDev &w, const void *X, long long n, float *y
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long tiles = (n + kRows - 1) / kRows;
     const long long grid = tiles < 2ll * sms ? tiles : 2ll * sms;
-    mlp_forward_tc_kernel<<<(unsigned) grid, kRows, kTcSmemBytes, s>>>(w, (const bf16 *) X, n, y, status);
+    mlp_tc_kernel<GRID><<<(unsigned) grid, kRows, kTcSmemBytes, s>>>(w, (const bf16 *) X, n, y, w.status, g);
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t mlp_forward_tc(const MlpDev &w, const void *X, long long n, float *y, int *status, cudaStream_t s)
+{
+    MlpDev ws = w;
+    ws.status = status;
+    return launch_tc<false>(ws, X, n, y, MlpGridArgs{}, s);
+}
+
+cudaError_t mlp_learned_grid_tc(const MlpDev &w, const MlpGridArgs &g, cudaStream_t s)
+{
+    return launch_tc<true>(w, nullptr, g.ncell, nullptr, g, s);
 }
 
 }  // namespace ivr
