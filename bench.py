@@ -437,10 +437,11 @@ def _methods(ctx, v, tfs, states, L, args, stream, device=0):
                                       judge_stride=args.judge_stride or L["judge_stride"])
                 view = vw[m].set(v, st, p)
                 torch.cuda.synchronize()
-                ev0.record(stream)
-                view.render(tf, None, outs[m].data_ptr(), sp)
-                ev1.record(stream)
-                torch.cuda.synchronize()
+                with nvtx_range(f"tf_edit_{m}"):  # the TF's grid build and first frame
+                    ev0.record(stream)
+                    view.render(tf, None, outs[m].data_ptr(), sp)
+                    ev1.record(stream)
+                    torch.cuda.synchronize()
                 first_ms[m].append(ev0.elapsed_time(ev1))
                 ev0.record(stream)
                 for _ in range(L["frames"]):
