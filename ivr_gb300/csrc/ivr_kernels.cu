@@ -5,6 +5,8 @@
 #include <float.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include <mutex>
 
 #include "ivr_internal.h"
@@ -188,24 +190,25 @@ __global__ void cell_opacity_kernel(const float *mc, int ncell, const double *ap
 // largest per-axis offset; anything farther than the cap is the cap).
 //
 // One pass over the lines along `axis` (0 = x, 1 = y, 2 = z), in place: a
-// block takes 32 neighbouring lines whole (neighbours along x for the y and
-// z passes, along y for the x pass), so that its loads and stores coalesce,
-// stages them in shared memory and writes them back once all are read.
+// block takes `lines` neighbouring lines whole (32, fewer for very long
+// lines; neighbours along x for the y and z passes, along y for the x
+// pass), so that its loads and stores coalesce, stages them in shared
+// memory and writes them back once all are read.
 constexpr int kDistLines = 32;
-__global__ void dist_axis_kernel(uint8_t *dist, int mcx, int mcy, int mcz, int axis)
+__global__ void dist_axis_kernel(uint8_t *dist, int mcx, int mcy, int mcz, int axis, int lines)
 {
-    extern __shared__ uint8_t tile[];  // [L][kDistLines + 1]
-    constexpr int P = kDistLines + 1;
+    extern __shared__ uint8_t tile[];  // [L][lines + 1]
+    const int P = lines + 1;
     const int L = axis == 0 ? mcx : axis == 1 ? mcy : mcz;
     const long long slab = (long long) mcx * mcy;
     const long long stride = axis == 0 ? 1 : axis == 1 ? mcx : slab;
     // this block's group of lines: the first line's base and the distance
     // between neighbouring lines; nl lines are in the grid
     const int across = axis == 0 ? mcy : mcx;  // lines of a group run along this dimension
-    const int groups_across = (across + kDistLines - 1) / kDistLines;
+    const int groups_across = (across + lines - 1) / lines;
     const long long g = blockIdx.x;
-    const int outer = (int) (g / groups_across), first = (int) (g % groups_across) * kDistLines;
-    const int nl = min(kDistLines, across - first);
+    const int outer = (int) (g / groups_across), first = (int) (g % groups_across) * lines;
+    const int nl = min(lines, across - first);
     long long base;
     long long step;
     if (axis == 0) {  // rows (y, z): outer = z, lines along y
@@ -455,11 +458,13 @@ cudaError_t launch_dist_transform(uint8_t *dist, int mcx, int mcy, int mcz, cuda
     for (int axis = 0; axis < 3; axis++) {
         const int L = dims[axis];
         if (L == 1) continue;  // a line of one cell keeps its flag
-        const size_t smem = (size_t) L * (kDistLines + 1);
-        if (smem > 48 * 1024) return cudaErrorInvalidValue;  // lines of more than 1489 cells
+        // 32 lines a block up to 1489 cells a line, fewer above
+        const int lines = std::min(kDistLines, 48 * 1024 / L - 1);
+        if (lines < 1) return cudaErrorInvalidValue;  // a line of more than 24576 macrocells
+        const size_t smem = (size_t) L * (lines + 1);
         const int across = axis == 0 ? mcy : mcx, outer = axis == 2 ? mcy : mcz;
-        const long long groups = (long long) outer * ((across + kDistLines - 1) / kDistLines);
-        dist_axis_kernel<<<(unsigned) groups, 256, smem, s>>>(dist, mcx, mcy, mcz, axis);
+        const long long groups = (long long) outer * ((across + lines - 1) / lines);
+        dist_axis_kernel<<<(unsigned) groups, 256, smem, s>>>(dist, mcx, mcy, mcz, axis, lines);
     }
     return cudaGetLastError();
 }

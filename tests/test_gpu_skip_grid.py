@@ -33,8 +33,10 @@ def chebyshev_capped(transparent):
     if len(opq) == 0:
         out[t] = CAP
         return out.astype(np.uint8)
-    d = np.abs(idx[:, None, :] - opq[None, :, :]).max(axis=2).min(axis=1).reshape(t.shape)
-    out = np.where(t, np.minimum(d, CAP), 0)
+    d = np.empty(len(idx), np.int64)
+    for a in range(0, len(idx), 512):  # all pairs, in chunks of cells
+        d[a:a + 512] = np.abs(idx[a:a + 512, None, :] - opq[None, :, :]).max(axis=2).min(axis=1)
+    out = np.where(t, np.minimum(d.reshape(t.shape), CAP), 0)
     return out.astype(np.uint8)
 
 
@@ -53,11 +55,11 @@ CASES = [
     ("u8", (40, 48, 36), 8, 5),
     ("f32", (36, 44, 40), 4, 7),
     ("u8", (8, 64, 60), 16, 11),   # one cell along z
+    ("u8", (8, 8, 6000), 4, 17),   # 1500 cells along x: fewer lines per block of the transform
 ]
 
 
-@pytest.mark.parametrize("dtype,shape,cell,seed", CASES, ids=[f"{c[0]}-{c[2]}" + ("-flat" if c[1][0] <= c[2] else "")
-                                                               for c in CASES])
+@pytest.mark.parametrize("dtype,shape,cell,seed", CASES, ids=["u16-8", "u8-8", "f32-4", "u8-16-flat", "u8-4-long"])
 def test_exact_grid_is_the_capped_distance_transform(ctx, oracle_mod, dtype, shape, cell, seed):
     vol = synth.blob_volume(shape, n_blobs=6, seed=seed, dtype=dtype, zero_fraction=0.4, cell=cell,
                             sigma_scale=0.7)
