@@ -9,6 +9,8 @@
 #include <float.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "ivr_internal.h"
 
 namespace ivr {
@@ -1184,11 +1186,14 @@ __global__ void sample_err_kernel(const __grid_constant__ FrameDesc f, SamplerTe
 template <typename K>
 int persistent_grid(K kernel, size_t smem)
 {
-    static int sms = 0;
+    // SM count of the current device, looked up once per device
+    static std::atomic<int> sm_count[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int sms = dev >= 0 && dev < 64 ? sm_count[dev].load(std::memory_order_relaxed) : 0;
     if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (dev >= 0 && dev < 64) sm_count[dev].store(sms, std::memory_order_relaxed);
     }
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);

@@ -472,11 +472,9 @@ cudaError_t mlp_forward(const MlpDev &w, const void *X, long long n, float *y, c
 cudaError_t mlp_train_step(const MlpDev &w, const void *X, const float *T, const int *idx, long long n,
                            long long n_total, float wneg, float gamma, float *grad, float *loss, cudaStream_t s)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sizeof(BwdSmem));
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    cudaError_t e = set_dynamic_smem_once(mlp_train_kernel, (int) sizeof(BwdSmem), attr);
+    if (e != cudaSuccess) return e;
     if (n <= 0) return cudaSuccess;
     mlp_train_kernel<<<(unsigned) ((n + R - 1) / R), R, sizeof(BwdSmem), s>>>(w, (const bf16 *) X, T, idx, n,
                                                                               n_total, wneg, gamma, grad, loss);

@@ -6,7 +6,25 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <atomic>
+
 namespace ivr {
+
+// cudaFuncSetAttribute(kernel, MaxDynamicSharedMemorySize, bytes) once per
+// device: the attribute belongs to the current device's context, so a flag
+// per device (bit dev of done) rather than one per process.
+template <typename K>
+inline cudaError_t set_dynamic_smem_once(K kernel, int bytes, std::atomic<unsigned long long> &done)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
+    return e;
+}
 
 constexpr int kMlpFeatures = 26;  // min, max, 8-bin histogram, 16 TF knots
 constexpr int kMlpIn = 32;        // padded input width

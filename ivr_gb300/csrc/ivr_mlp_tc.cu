@@ -317,13 +317,9 @@ namespace {
 template <bool GRID>
 cudaError_t launch_tc(const MlpDev &w, const void *X, long long n, float *y, const MlpGridArgs &g, cudaStream_t s)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel<GRID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int) kTcSmemBytes);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    cudaError_t e = set_dynamic_smem_once(mlp_tc_kernel<GRID>, (int) kTcSmemBytes, attr);
+    if (e != cudaSuccess) return e;
     if (n <= 0) return cudaSuccess;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
