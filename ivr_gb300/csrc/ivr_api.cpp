@@ -270,16 +270,13 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, bool learned, cuda
     g->rejected = false;
     *(volatile int *) g->h_reject = 0;  // no launch that reads it is pending
     CK(c, cudaMemsetAsync(g->d_bad, 0, sizeof(int), s));
-    for (size_t k = 0; k < v->bricks.size(); k++) {
-        const HostBrick &b = v->bricks[k];
-        if (zero_alpha)
-            CK(c, cudaMemsetAsync(g->opac[k], 0, mc_cells(b), s));
-        else
-            CK(c, launch_cell_opacity(b.mc_minmax, b.mcx, b.mcy, b.mcz, tf->d_aprefix, tf->n, tf->off, tf->scale,
-                                      g->opac[k], s));
-    }
+    // cell opacities (the tile order's input): an exact grid's only; learned
+    // frames use those of their TF's exact grid
     if (zero_alpha) {
-        for (size_t k = 0; k < v->bricks.size(); k++) CK(c, cudaMemsetAsync(g->dist[k], kDistCap, mc_cells(v->bricks[k]), s));
+        for (size_t k = 0; k < v->bricks.size(); k++) {
+            CK(c, cudaMemsetAsync(g->opac[k], 0, mc_cells(v->bricks[k]), s));
+            CK(c, cudaMemsetAsync(g->dist[k], kDistCap, mc_cells(v->bricks[k]), s));
+        }
     } else if (learned) {
         int rc = learned_fields(v, tf, g->dist, s);
         if (rc) {
@@ -290,8 +287,8 @@ int tf_grid(ivr_volume *v, const ivr_tf *tf, bool zero_alpha, bool learned, cuda
     } else {
         for (size_t k = 0; k < v->bricks.size(); k++) {
             const HostBrick &b = v->bricks[k];
-            CK(c, launch_empty_flags(b.mc_minmax, b.mcx, b.mcy, b.mcz, tf->d_nzprefix, tf->n, tf->off, tf->scale,
-                                     g->dist[k], s));
+            CK(c, launch_empty_flags(b.mc_minmax, b.mcx, b.mcy, b.mcz, tf->d_nzprefix, tf->d_aprefix, tf->n, tf->off,
+                                     tf->scale, g->dist[k], g->opac[k], s));
         }
     }
     CK(c, cudaEventRecord(g->ev, s));
@@ -362,23 +359,26 @@ int frame_for(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int single
         // fallback's), unless the judge has rejected it: then only the exact
         const bool zero_alpha = !(f.alpha != 0.0f);
         bool learned = view->p.skip == IVR_SKIP_LEARNED && !zero_alpha;
-        ivr_volume::TfGrid *lg = nullptr;
-        if (learned) {
-            if (!exact) return fail(view->ctx, IVR_ERR_UNSUPPORTED, "IVR_SKIP_LEARNED frames render through ivr_render*");
-            int rc = tf_grid(view->vol, tf, false, true, s, protect_from, &lg, built);
-            if (rc) return rc;
-            learned = !learned_rejected(lg);
-        }
+        if (learned && !exact)
+            return fail(view->ctx, IVR_ERR_UNSUPPORTED, "IVR_SKIP_LEARNED frames render through ivr_render*");
+        // the exact grid first: its cell opacities (the tile order's input,
+        // the same for both grids of a TF) serve the learned frames too
         ivr_volume::TfGrid *eg = nullptr;
         bool ebuilt = false;
         int rc = tf_grid(view->vol, tf, zero_alpha, false, s, protect_from, &eg, &ebuilt);
         if (rc) return rc;
+        ivr_volume::TfGrid *lg = nullptr;
+        if (learned) {
+            rc = tf_grid(view->vol, tf, false, true, s, protect_from, &lg, built);
+            if (rc) return rc;
+            learned = !learned_rejected(lg);
+        }
         if (built) *built |= ebuilt;
         *grid = learned ? lg : eg;
         if (learned) *exact = eg;
         for (int k = 0; k < f.nb; k++) {
             f.b[k].empty = (*grid)->dist[k];
-            f.b[k].opac = (*grid)->opac[k];
+            f.b[k].opac = eg->opac[k];
         }
     }
     return IVR_OK;
@@ -408,9 +408,11 @@ int launch_view(ivr_view *view, FrameDesc &f, float *o32, uint8_t *o8, cudaStrea
 // IVR_TILES_COST: the launch's tile permutation, costliest first, into the
 // view's next slot (grown to the window's tile count); sets f.perm and
 // returns the slot.  Built on the view's order stream after the launches
-// that last read the slot and after the grid's build, so it overlaps the
-// tail of the frame before (in a stream capture: on s itself).
-int order_tiles(ivr_view *view, FrameDesc &f, const ivr_volume::TfGrid *grid, cudaStream_t s, int *slot)
+// that last read the slot and after the builds of the grid and of the exact
+// grid (whose cell opacities it reads), so it overlaps the tail of the
+// frame before (in a stream capture: on s itself).
+int order_tiles(ivr_view *view, FrameDesc &f, const ivr_volume::TfGrid *grid, const ivr_volume::TfGrid *exact,
+                cudaStream_t s, int *slot)
 {
     ivr_ctx *c = view->ctx;
     const long long ntiles = (long long) ((f.out_w + 7) >> 3) * ((f.out_h + 3) >> 2);
@@ -468,6 +470,7 @@ int order_tiles(ivr_view *view, FrameDesc &f, const ivr_volume::TfGrid *grid, cu
     if (os != s) {
         if (o.used_recorded) CK(c, cudaStreamWaitEvent(os, o.used, 0));
         CK(c, cudaStreamWaitEvent(os, grid->built, 0));
+        if (exact) CK(c, cudaStreamWaitEvent(os, exact->built, 0));  // its cell opacities
     }
     CK(c, launch_tile_order(f, o.key, o.counts, o.perm, os));
     if (os != s) {
@@ -518,7 +521,7 @@ int render_window(ivr_view *view, ivr_tf *tf, int x, int y, int w, int h, int si
     }
     int slot = -1;
     if (!touched && grid && view->p.tile_order == IVR_TILES_COST) {
-        rc = order_tiles(view, f, grid, s, &slot);
+        rc = order_tiles(view, f, grid, exact, s, &slot);
         if (rc) return rc;
     }
     rc = launch_view(view, f, o32, o8, s);

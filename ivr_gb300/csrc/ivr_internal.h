@@ -150,8 +150,11 @@ cudaError_t launch_histogram(const void *data, int dtype, long long n, float mn,
                              cudaStream_t s);
 cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int nz, int cell, float *mc, int mcx,
                               int mcy, int mcz, cudaStream_t s);
-cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const int *nzprefix, int lut_n,
-                               int lut_off, float lut_scale, uint8_t *empty, cudaStream_t s);
+// a TF's exact grid: the empty-cell flags, then the distance transform; with
+// opac, each cell's 255 sqrt(mean LUT opacity over its value range) as well
+// (DevBrick::opac, the tile cost estimate's input)
+cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const int *nzprefix, const double *aprefix,
+                               int lut_n, int lut_off, float lut_scale, uint8_t *empty, uint8_t *opac, cudaStream_t s);
 // per-voxel gradient (gx, gy, gz, |g|) of a w x h x d volume into out
 cudaError_t launch_gradient(const void *data, int dtype, int w, int h, int d, float4 *out, cudaStream_t s);
 // corner-packed copy of an nx x ny x nz brick: (nx-1)(ny-1)nz four-voxel
@@ -196,9 +199,6 @@ long long judge_scratch_bytes(const FrameDesc &f);
 cudaError_t launch_tile_order(const FrameDesc &f, uint8_t *key, int *counts, int *perm, cudaStream_t s);
 // the capped distance transform of a flag grid (kDistCap or 0 per cell), in place
 cudaError_t launch_dist_transform(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s);
-// per macrocell 255 sqrt(mean LUT opacity over its value range) (DevBrick::opac)
-cudaError_t launch_cell_opacity(const float *mc, int mcx, int mcy, int mcz, const double *aprefix, int lut_n,
-                                int lut_off, float lut_scale, uint8_t *opac, cudaStream_t s);
 // batched CONFIG frames of one volume dtype; *ticket must be zero at launch
 cudaError_t launch_batch(int dtype, int variant, const BatchHeader *hdr, const BatchItem *items,
                          unsigned long long *ticket, cudaStream_t s);

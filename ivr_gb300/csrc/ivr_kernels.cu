@@ -148,34 +148,26 @@ __global__ void macrocell_kernel(const void *data, int dtype, int nx, int ny, in
 // non-zero opacity.  Samples lie in [min, max] of the cell's voxels up to
 // rounding, so the index range is widened by one on each side.
 // nzprefix[i] = number of entries in [0, i) with non-zero opacity.
-// Writes kDistCap for a transparent cell and 0 for the others.
-__global__ void empty_kernel(const float *mc, int ncell, const int *nzprefix, int lut_n, int lut_off,
-                             float lut_scale, uint8_t *dist)
+// Writes kDistCap for a transparent cell and 0 for the others.  In the same
+// pass (opac non-null), the tile cost estimate's input: 255 sqrt(mean LUT
+// opacity over the entries the cell's voxel range [min, max] indexes); the
+// square root keeps small opacities apart; aprefix[i] = sum of the
+// opacities of entries [0, i).
+__global__ void empty_kernel(const float *mc, int ncell, const int *nzprefix, const double *aprefix, int lut_n,
+                             int lut_off, float lut_scale, uint8_t *dist, uint8_t *opac)
 {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
-        int lo = (int) (mc[2 * c] * lut_scale) - 1 - lut_off;
-        int hi = (int) (mc[2 * c + 1] * lut_scale) + 1 - lut_off;
-        lo = min(max(lo, 0), lut_n - 1);
-        hi = min(max(hi, 0), lut_n - 1);
+        const int i0 = (int) (mc[2 * c] * lut_scale) - lut_off, i1 = (int) (mc[2 * c + 1] * lut_scale) - lut_off;
+        const int lo = min(max(i0 - 1, 0), lut_n - 1);
+        const int hi = min(max(i1 + 1, 0), lut_n - 1);
         dist[c] = (nzprefix[hi + 1] - nzprefix[lo]) == 0 ? (uint8_t) kDistCap : 0;
-    }
-}
-
-// Per cell, 255 sqrt(mean LUT opacity over the entries its voxel range
-// [min, max] indexes) -- the input of the tile cost estimate; the square
-// root keeps small opacities apart.  aprefix[i] = sum of the opacities of
-// entries [0, i).
-__global__ void cell_opacity_kernel(const float *mc, int ncell, const double *aprefix, int lut_n, int lut_off,
-                                    float lut_scale, uint8_t *opac)
-{
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
-        int lo = (int) (mc[2 * c] * lut_scale) - lut_off;
-        int hi = (int) (mc[2 * c + 1] * lut_scale) - lut_off;
-        lo = min(max(lo, 0), lut_n - 1);
-        hi = min(max(hi, lo), lut_n - 1);
-        const double mean = (aprefix[hi + 1] - aprefix[lo]) / (double) (hi - lo + 1);
-        const float q = sqrtf(fminf(fmaxf((float) mean, 0.0f), 1.0f)) * 255.0f + 0.5f;
-        opac[c] = (uint8_t) min((int) q, 255);
+        if (opac) {
+            const int a = min(max(i0, 0), lut_n - 1);
+            const int b = min(max(i1, a), lut_n - 1);
+            const double mean = (aprefix[b + 1] - aprefix[a]) / (double) (b - a + 1);
+            const float q = sqrtf(fminf(fmaxf((float) mean, 0.0f), 1.0f)) * 255.0f + 0.5f;
+            opac[c] = (uint8_t) min((int) q, 255);
+        }
     }
 }
 
@@ -435,20 +427,13 @@ cudaError_t launch_macrocells(const void *data, int dtype, int nx, int ny, int n
     return cudaGetLastError();
 }
 
-cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const int *nzprefix, int lut_n,
-                               int lut_off, float lut_scale, uint8_t *empty, cudaStream_t s)
+cudaError_t launch_empty_flags(const float *mc, int mcx, int mcy, int mcz, const int *nzprefix, const double *aprefix,
+                               int lut_n, int lut_off, float lut_scale, uint8_t *empty, uint8_t *opac, cudaStream_t s)
 {
     const int ncell = mcx * mcy * mcz;
-    empty_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mc, ncell, nzprefix, lut_n, lut_off, lut_scale, empty);
+    empty_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mc, ncell, nzprefix, aprefix, lut_n, lut_off, lut_scale, empty,
+                                                      opac);
     return launch_dist_transform(empty, mcx, mcy, mcz, s);
-}
-
-cudaError_t launch_cell_opacity(const float *mc, int mcx, int mcy, int mcz, const double *aprefix, int lut_n,
-                                int lut_off, float lut_scale, uint8_t *opac, cudaStream_t s)
-{
-    const int ncell = mcx * mcy * mcz;
-    cell_opacity_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mc, ncell, aprefix, lut_n, lut_off, lut_scale, opac);
-    return cudaGetLastError();
 }
 
 cudaError_t launch_dist_transform(uint8_t *dist, int mcx, int mcy, int mcz, cudaStream_t s)

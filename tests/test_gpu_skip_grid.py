@@ -13,6 +13,8 @@ calls transparent, must be the distance transform of its own transparent
 set, and must equal the grid built from the same steps run one by one
 (ivr_mlp_features, ivr_mlp_forward, the margin and the exact test).
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -144,4 +146,31 @@ def test_learned_grid_is_certified_and_its_own_distance_transform(ctx, oracle_mo
         mlp.free()
         for tf in tfs:
             tf.free()
+        v.free()
+
+
+def test_skip_grid_arguments(ctx):
+    """Wrong arguments are errors with a message, not faults: a skip mode
+    without a grid, a brick out of range, an output too small; a learned
+    grid needs a predictor."""
+    vol = synth.blob_volume((32, 32, 32), n_blobs=4, seed=2, dtype="u8")
+    v = ctx.load_volume(vol).macrocell(8)
+    tf = ctx.transfer_function().set_lut(synth.ramp_tf(), 0, 1.0, api.TF_F2B)
+    lib = ctx.lib
+    try:
+        dims = (ctypes.c_int * 3)()
+        for skip, brick, n, why in ((api.SKIP_NONE, 0, 64, "skip"), (api.SKIP_GRID, 1, 64, "brick"),
+                                    (api.SKIP_GRID, -1, 64, "brick"), (api.SKIP_GRID, 0, 63, "bytes")):
+            buf = np.zeros(max(n, 1), np.uint8)
+            rc = lib.ivr_volume_skip_grid(v.h, tf.h, skip, brick, buf.ctypes.data, n, dims)
+            assert rc != 0, why
+            assert lib.ivr_last_error(ctx.h).decode(), why
+        assert lib.ivr_volume_skip_grid(v.h, tf.h, api.SKIP_GRID, 0, None, 0, dims) == 0
+        assert tuple(dims) == (4, 4, 4)
+        with pytest.raises(api.IvrError):
+            v.skip_grid(tf, api.SKIP_LEARNED)  # no predictor attached
+        g = v.skip_grid(tf, api.SKIP_GRID)  # the context still works
+        assert g.shape == (4, 4, 4)
+    finally:
+        tf.free()
         v.free()
