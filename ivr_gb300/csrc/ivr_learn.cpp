@@ -34,7 +34,7 @@ struct ivr_mlp {
     long long loss_cap = 0;
     float *d_knots = nullptr;  // the knots of the TF whose learned grid is being built
     int *d_key = nullptr;
-    int *d_status = nullptr;  // inference status word (kMlpTcTimeout)
+    int *d_status = nullptr;  // tensor-core status word (kMlpTcTimeout): training, inference, grids
     unsigned long long *d_counts = nullptr;
     cudaEvent_t scratch_ev = nullptr;  // after the last use of d_knots
 };
@@ -461,6 +461,12 @@ int ivr_mlp_train(ivr_mlp *m, int epochs, int batch_rows, float lr, float wneg, 
         }
     }
     m->serial++;
+    int status = 0;
+    CK(c, cudaMemcpy(&status, m->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status != 0) {
+        cudaMemset(m->d_status, 0, sizeof(int));
+        return fail(c, IVR_ERR_TIMEOUT, "a tensor-core wait of the training step ran out; the parameters are suspect");
+    }
     return IVR_OK;
 }
 

@@ -52,13 +52,12 @@ struct MlpDev {
 };
 constexpr int kMlpTcTimeout = 1;
 
-size_t mlp_forward_smem();
-size_t mlp_train_smem();
-// inference: y for rows 0..n of X, on the tcgen05 tensor cores (ivr_mlp_tc.cu)
+// inference: y for rows 0..n of X, on the tcgen05 tensor cores (ivr_mlp_tc.cu);
+// a wait that runs out records kMlpTcTimeout in *w.status
 cudaError_t mlp_forward(const MlpDev &w, const void *X, long long n, float *y, cudaStream_t s);
-cudaError_t mlp_forward_tc(const MlpDev &w, const void *X, long long n, float *y, int *status, cudaStream_t s);
-// forward + backward over rows idx[0..n) (idx null: rows 0..n), gradients
-// added into grad, loss into *loss; targets <= 0 are one-sided (gamma)
+// forward + backward over rows idx[0..n) (idx null: rows 0..n) on tcgen05,
+// gradients added into grad, loss into *loss; targets <= 0 are one-sided
+// (gamma) (ivr_mlp_tc.cu)
 cudaError_t mlp_train_step(const MlpDev &w, const void *X, const float *T, const int *idx, long long n,
                            long long n_total, float wneg, float gamma, float *grad, float *loss, cudaStream_t s);
 // Adam step `step` (1-based) on the FP32 parameters, then the BF16 copies
