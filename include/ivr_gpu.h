@@ -352,9 +352,8 @@ int ivr_server_listen(ivr_server *server, int port, int volume, int tf, int *bou
  *     TF's 16 knots: the largest LUT opacity over each sixteenth of the
  *     volume's value range;
  *   network: 26 -> 64 -> 64 -> 1, ReLU, BF16 weights and activations, FP32
- *     accumulation on the tensor cores (inference and the grid of a TF in
- *     one tcgen05 launch with accumulators in tensor memory; training with
- *     warp-level MMA);
+ *     accumulation on the tcgen05 tensor cores with accumulators in tensor
+ *     memory (training, inference, and the grid of a TF in one launch);
  *   target: the exact bound the plain grid uses, the largest LUT opacity
  *     over the index range of the cell's values.  A cell whose bound is 0
  *     costs only when y > -IVR_MLP_TRANSPARENT; otherwise the loss is
