@@ -118,6 +118,25 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// A ROWS x K BF16 matrix, row-major in global memory, into a canonical
+// K-major tile: 16-byte chunks (8 elements of a row), all of a thread's
+// loads issued before its stores (the trip count is a constant).
+template <int ROWS, int K>
+__device__ __forceinline__ void stage_kmajor(unsigned char *dst, const void *src, int sbo)
+{
+    constexpr int kChunks = ROWS * (K / 8), kPer = kChunks / kRows;
+    static_assert(kChunks % kRows == 0, "whole chunks per thread");
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    uint4 v[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; j++) v[j] = __ldg(s4 + threadIdx.x + j * kRows);
+#pragma unroll
+    for (int j = 0; j < kPer; j++) {
+        const int i = threadIdx.x + j * kRows;
+        *reinterpret_cast<uint4 *>(dst + kmajor_off(i / (K / 8), 8 * (i % (K / 8)), sbo)) = v[j];
+    }
+}
+
 __device__ __forceinline__ uint32_t pack2(float a, float b)
 {
     const bf16 lo = __float2bfloat16(a), hi = __float2bfloat16(b);
@@ -135,14 +154,8 @@ __global__ void __launch_bounds__(kRows) mlp_tc_kernel(MlpDev w, const bf16 *X, 
     const int tid = threadIdx.x, warp = tid >> 5;
     // weights and biases, once per block, in the operand layouts
     const bf16 *w1t = (const bf16 *) w.w1t, *w2t = (const bf16 *) w.w2t;
-    for (int i = tid; i < kHid * kIn; i += kRows) {
-        const int r = i / kIn, k = i % kIn;
-        *reinterpret_cast<bf16 *>(s.w1 + kmajor_off(r, k, kSbo1)) = w1t[i];
-    }
-    for (int i = tid; i < kHid * kHid; i += kRows) {
-        const int r = i / kHid, k = i % kHid;
-        *reinterpret_cast<bf16 *>(s.w2 + kmajor_off(r, k, kSbo2)) = w2t[i];
-    }
+    stage_kmajor<kHid, kIn>(s.w1, w1t, kSbo1);
+    stage_kmajor<kHid, kHid>(s.w2, w2t, kSbo2);
     for (int i = tid; i < kHid; i += kRows) {
         s.b1[i] = w.b1[i];
         s.b2[i] = w.b2[i];
@@ -389,12 +402,9 @@ __global__ void __launch_bounds__(kRows) mlp_train_tc_kernel(MlpDev w, const bf1
     const int tid = threadIdx.x, warp = tid >> 5;
     // weights in their operand layouts, biases, zeroed sums and padding rows
     const bf16 *w1t = (const bf16 *) w.w1t, *w2t = (const bf16 *) w.w2t, *w2 = (const bf16 *) w.w2;
-    for (int i = tid; i < kHid * kIn; i += kRows)
-        *reinterpret_cast<bf16 *>(s.w1 + kmajor_off(i / kIn, i % kIn, kSbo1)) = w1t[i];
-    for (int i = tid; i < kHid * kHid; i += kRows) {
-        *reinterpret_cast<bf16 *>(s.w2t + kmajor_off(i / kHid, i % kHid, kSbo2)) = w2t[i];
-        *reinterpret_cast<bf16 *>(s.w2 + kmajor_off(i / kHid, i % kHid, kSbo2)) = w2[i];
-    }
+    stage_kmajor<kHid, kIn>(s.w1, w1t, kSbo1);
+    stage_kmajor<kHid, kHid>(s.w2t, w2t, kSbo2);
+    stage_kmajor<kHid, kHid>(s.w2, w2, kSbo2);
     for (int i = tid; i < kHid; i += kRows) {
         s.b1[i] = w.b1[i];
         s.b2[i] = w.b2[i];
