@@ -1025,24 +1025,33 @@ __global__ void __launch_bounds__(kThreads, JUDGE ? kJudgeBlocksPerSm : kCfgBloc
         if (lane == 0) ticket = atomicAdd(f.tickets, 1ull);
         const long long q = (long long) (__shfl_sync(0xffffffffu, ticket, 0) - f.ticket_base);
         if (q >= ntiles + njudged) break;
-        if (JUDGE && q < njudged) {
-            if (exact) continue;
-            const long long tile = q * f.judge_stride + f.judge_phase;
-            const int oi = (int) (tile / tiles_x) * 4 + (lane >> 3), oj = (int) (tile % tiles_x) * 8 + (lane & 7);
-            const int i = f.out_y + oi, j = f.out_x + oj;
-            float4 ex = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (oi < f.out_h && oj < f.out_w && i < f.vh && j < f.vw)
-                ex = ray_cfg<DT, true, false, kPair>(f, i, j, nexec, nlat, true);
-            f.judge8[q * 32 + lane] = make_uchar4(q8(ex.x), q8(ex.y), q8(ex.z), q8(ex.w));
-            continue;
-        }
-        long long tile = q - njudged;
-        if (f.perm != nullptr) {
-            const long long p = f.perm[tile];
-            if (p >= 0 && p < ntiles) tile = p;  // a permutation by construction; never leave the window
+        // a judged tile (re-marched with the exact grids into judge8) or a
+        // render tile, through one copy of the march
+        const bool judge = JUDGE && q < njudged;
+        if (judge && exact) continue;
+        long long tile;
+        if (judge) {
+            tile = q * f.judge_stride + f.judge_phase;
+        } else {
+            tile = q - njudged;
+            if (f.perm != nullptr) {
+                const long long p = f.perm[tile];
+                if (p >= 0 && p < ntiles) tile = p;  // a permutation by construction; never leave the window
+            }
         }
         const int oi = (int) (tile / tiles_x) * 4 + (lane >> 3), oj = (int) (tile % tiles_x) * 8 + (lane & 7);
-        pixel_cfg<DT, SKIP, CENSUS, kPair>(f, oi, oj, out32, out8, nexec, nlat, exact);
+        const bool in_window = oi < f.out_h && oj < f.out_w;
+        const int i = f.out_y + oi, j = f.out_x + oj;
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (in_window && i < f.vh && j < f.vw) acc = ray_cfg<DT, SKIP, CENSUS, kPair>(f, i, j, nexec, nlat, judge || exact);
+        const uchar4 a8 = make_uchar4(q8(acc.x), q8(acc.y), q8(acc.z), q8(acc.w));
+        if (judge) {
+            f.judge8[q * 32 + lane] = a8;
+        } else if (in_window) {
+            const long long o = (long long) oi * f.out_w + oj;
+            if (out32) out32[o] = acc;
+            if (out8) out8[o] = a8;
+        }
     }
     if (CENSUS) count_exec(f, nexec, nlat);
 }
