@@ -149,6 +149,46 @@ int features(ivr_mlp *m, ivr_volume *v, const ivr_tf *tf, uint16_t *X, float *T,
 
 }  // namespace
 
+namespace {
+
+// splitmix64: the training order's random stream (seeded per predictor)
+struct SplitMix {
+    uint64_t x;
+    uint64_t next()
+    {
+        uint64_t z = (x += 0x9e3779b97f4a7c15ull);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        return z ^ (z >> 31);
+    }
+    // uniform in [0, bound), bound < 2^32: the multiply-shift reduction with
+    // rejection of the biased low range (Lemire)
+    uint32_t below(uint32_t bound)
+    {
+        uint64_t m = (next() >> 32) * (uint64_t) bound;
+        uint32_t lo = (uint32_t) m;
+        if (lo < bound) {
+            const uint32_t t = (uint32_t) (-bound) % bound;
+            while (lo < t) {
+                m = (next() >> 32) * (uint64_t) bound;
+                lo = (uint32_t) m;
+            }
+        }
+        return (uint32_t) (m >> 32);
+    }
+};
+
+// Fisher-Yates over a[0..n)
+void shuffle_rows(int *a, size_t n, SplitMix &rng)
+{
+    for (size_t i = n; i > 1; i--) {
+        const size_t j = rng.below((uint32_t) i);
+        std::swap(a[i - 1], a[j]);
+    }
+}
+
+}  // namespace
+
 unsigned ivr::mlp_serial(const ivr_mlp *m) { return m->serial; }
 
 void ivr::learned_release(ivr_volume *v)
@@ -436,38 +476,102 @@ int ivr_mlp_train(ivr_mlp *m, int epochs, int batch_rows, float lr, float wneg, 
     const long long nb = (m->n + batch_rows - 1) / batch_rows;
     int rc = grow(c, (void **) &m->d_loss, &m->loss_cap, nb, sizeof(float), 0);
     if (rc) return rc;
-    const MlpDev w = dev_of(m);
-    std::vector<int> perm((size_t) m->n);
-    std::iota(perm.begin(), perm.end(), 0);
-    std::mt19937_64 rng(m->seed ^ 0x9e3779b97f4a7c15ull);
-    std::vector<float> losses((size_t) nb);
-    CK(c, cudaDeviceSynchronize());
-    for (int e = 0; e < epochs; e++) {
-        std::shuffle(perm.begin(), perm.end(), rng);
-        CK(c, cudaMemcpy(m->d_idx, perm.data(), sizeof(int) * perm.size(), cudaMemcpyHostToDevice));
-        CK(c, cudaMemsetAsync(m->d_loss, 0, sizeof(float) * (size_t) nb, 0));
-        for (long long b = 0; b < nb; b++) {
-            const long long r0 = b * batch_rows, rows = std::min<long long>(batch_rows, m->n - r0);
-            CK(c, cudaMemsetAsync(m->d_grad, 0, kParamBytes, 0));
-            CK(c, mlp_train_step(w, m->d_X, m->d_T, m->d_idx + r0, rows, rows, wneg, IVR_MLP_TRANSPARENT, m->d_grad,
-                                 m->d_loss + b, 0));
-            CK(c, mlp_adam(m->d_p, m->d_m, m->d_v, m->d_grad, lr, ++m->step, m->d_w1t, m->d_w2t, m->d_w2, 0));
+    // the Adam bias corrections of an epoch's steps, device-resident so that
+    // one captured epoch replays with each epoch's values
+    float *d_c12 = nullptr;
+    rc = dev_alloc(c, sizeof(float) * 2 * (size_t) nb, (void **) &d_c12);
+    if (rc) return rc;
+    struct Graph {
+        cudaStream_t s = nullptr;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t x = nullptr;
+        ~Graph()
+        {
+            if (x) cudaGraphExecDestroy(x);
+            if (g) cudaGraphDestroy(g);
+            if (s) cudaStreamDestroy(s);
         }
-        CK(c, cudaMemcpy(losses.data(), m->d_loss, sizeof(float) * (size_t) nb, cudaMemcpyDeviceToHost));
+    } gr;
+    auto done = [&](int code) {
+        dev_free(c, d_c12, sizeof(float) * 2 * (size_t) nb);
+        return code;
+    };
+    const MlpDev w = dev_of(m);
+    // the epochs' row orders in two page-locked buffers: the host shuffles
+    // the next epoch's while the device trains on the current one
+    const size_t n = (size_t) m->n;
+    int *order[2] = {nullptr, nullptr};
+    struct Pinned {
+        int **p;
+        ~Pinned()
+        {
+            for (int k = 0; k < 2; k++)
+                if (p[k]) cudaFreeHost(p[k]);
+        }
+    } pinned{order};
+    SplitMix rng{m->seed ^ 0x9e3779b97f4a7c15ull};
+    std::vector<float> losses((size_t) nb), c12((size_t) (2 * nb));
+    cudaError_t e = cudaDeviceSynchronize();
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) e = cudaHostAlloc((void **) &order[k], sizeof(int) * n, 0);
+    if (e != cudaSuccess) return done(cuda_fail(c, e, "training order buffers"));
+    for (size_t i = 0; i < n; i++) order[0][i] = (int) i;
+    shuffle_rows(order[0], n, rng);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&gr.s, cudaStreamNonBlocking);
+    // the kernels' shared-memory attributes, set outside the capture
+    if (e == cudaSuccess) e = mlp_train_step(w, m->d_X, m->d_T, m->d_idx, 0, 1, wneg, IVR_MLP_TRANSPARENT, m->d_grad,
+                                             m->d_loss, gr.s);
+    // one epoch's mini-batches: gradient reset, training step, Adam (a
+    // launch-bound loop of 3 x nb launches, captured once)
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(gr.s, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t ce = cudaSuccess;
+        for (long long b = 0; b < nb && ce == cudaSuccess; b++) {
+            const long long r0 = b * batch_rows, rows = std::min<long long>(batch_rows, m->n - r0);
+            ce = cudaMemsetAsync(m->d_grad, 0, kParamBytes, gr.s);
+            if (ce == cudaSuccess)
+                ce = mlp_train_step(w, m->d_X, m->d_T, m->d_idx + r0, rows, rows, wneg, IVR_MLP_TRANSPARENT, m->d_grad,
+                                    m->d_loss + b, gr.s);
+            if (ce == cudaSuccess)
+                ce = mlp_adam(m->d_p, m->d_m, m->d_v, m->d_grad, lr, 0, d_c12 + 2 * b, m->d_w1t, m->d_w2t, m->d_w2,
+                              gr.s);
+        }
+        e = cudaStreamEndCapture(gr.s, &gr.g);
+        if (e == cudaSuccess) e = ce;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&gr.x, gr.g, 0);
+    if (e != cudaSuccess) return done(cuda_fail(c, e, "training graph"));
+    for (int ep = 0; ep < epochs; ep++) {
+        const int cur = ep & 1;
+        for (long long b = 0; b < nb; b++) mlp_adam_corrections(m->step + b + 1, &c12[2 * b], &c12[2 * b + 1]);
+        e = cudaMemcpyAsync(m->d_idx, order[cur], sizeof(int) * n, cudaMemcpyHostToDevice, gr.s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_c12, c12.data(), sizeof(float) * c12.size(), cudaMemcpyHostToDevice, gr.s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m->d_loss, 0, sizeof(float) * (size_t) nb, gr.s);
+        if (e == cudaSuccess) e = cudaGraphLaunch(gr.x, gr.s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(losses.data(), m->d_loss, sizeof(float) * (size_t) nb, cudaMemcpyDeviceToHost, gr.s);
+        if (e == cudaSuccess && ep + 1 < epochs) {  // the next epoch's order, meanwhile
+            memcpy(order[cur ^ 1], order[cur], sizeof(int) * n);
+            shuffle_rows(order[cur ^ 1], n, rng);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(gr.s);  // c12 and the order buffers are rewritten next
+        if (e != cudaSuccess) return done(cuda_fail(c, e, "training epoch"));
+        m->step += (int) nb;
         if (loss_per_epoch) {
             double sum = 0.0;
             for (float l : losses) sum += l;
-            loss_per_epoch[e] = (float) (sum / (double) nb);
+            loss_per_epoch[ep] = (float) (sum / (double) nb);
         }
     }
     m->serial++;
     int status = 0;
-    CK(c, cudaMemcpy(&status, m->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    e = cudaMemcpy(&status, m->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return done(cuda_fail(c, e, "training status"));
     if (status != 0) {
         cudaMemset(m->d_status, 0, sizeof(int));
-        return fail(c, IVR_ERR_TIMEOUT, "a tensor-core wait of the training step ran out; the parameters are suspect");
+        return done(fail(c, IVR_ERR_TIMEOUT, "a tensor-core wait of the training step ran out; the parameters are suspect"));
     }
-    return IVR_OK;
+    return done(IVR_OK);
 }
 
 int ivr_mlp_calibrate(ivr_mlp *m, float slack, float *margin, float *recall)

@@ -20,9 +20,16 @@ constexpr int F = kMlpIn;      // 32 (26 features, zero padded)
 constexpr int H = kMlpHidden;  // 64
 
 // Adam on the FP32 master parameters, then the BF16 operand copies
+// c12 (nullable): the bias corrections c1, c2 read from device memory
+// instead of the arguments (a launch that a CUDA graph replays every epoch)
 __global__ void mlp_adam_kernel(float *p, float *m, float *v, const float *gr, int np, float lr, float beta1,
-                                float beta2, float eps, float c1, float c2, bf16 *w1t, bf16 *w2t, bf16 *w2)
+                                float beta2, float eps, float c1, float c2, const float *c12, bf16 *w1t, bf16 *w2t,
+                                bf16 *w2)
 {
+    if (c12) {
+        c1 = c12[0];
+        c2 = c12[1];
+    }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
         float gi = gr[i];
         if (i >= kOffW1 + kMlpFeatures * H && i < kOffW1 + F * H) gi = 0.0f;  // padding inputs
@@ -169,13 +176,20 @@ int grid_of(long long n, int threads)
 
 }  // namespace
 
-cudaError_t mlp_adam(float *p, float *m, float *v, const float *grad, float lr, int step, void *w1t, void *w2t,
-                     void *w2, cudaStream_t s)
+void mlp_adam_corrections(long long step, float *c1, float *c2)
+{
+    *c1 = 1.0f - powf(0.9f, (float) step);
+    *c2 = 1.0f - powf(0.999f, (float) step);
+}
+
+cudaError_t mlp_adam(float *p, float *m, float *v, const float *grad, float lr, int step, const float *c12,
+                     void *w1t, void *w2t, void *w2, cudaStream_t s)
 {
     const float b1 = 0.9f, b2 = 0.999f;
-    const float c1 = 1.0f - powf(b1, (float) step), c2 = 1.0f - powf(b2, (float) step);
+    float c1 = 1.0f, c2 = 1.0f;
+    if (!c12) mlp_adam_corrections(step, &c1, &c2);
     mlp_adam_kernel<<<grid_of(kMlpParams, 256), 256, 0, s>>>(p, m, v, grad, kMlpParams, lr, b1, b2, 1e-8f, c1, c2,
-                                                             (bf16 *) w1t, (bf16 *) w2t, (bf16 *) w2);
+                                                             c12, (bf16 *) w1t, (bf16 *) w2t, (bf16 *) w2);
     mlp_pack_kernel<<<grid_of(F * H + H * H, 256), 256, 0, s>>>(p, (bf16 *) w1t, (bf16 *) w2t, (bf16 *) w2);
     return cudaGetLastError();
 }

@@ -60,9 +60,12 @@ cudaError_t mlp_forward(const MlpDev &w, const void *X, long long n, float *y, c
 // (gamma) (ivr_mlp_tc.cu)
 cudaError_t mlp_train_step(const MlpDev &w, const void *X, const float *T, const int *idx, long long n,
                            long long n_total, float wneg, float gamma, float *grad, float *loss, cudaStream_t s);
-// Adam step `step` (1-based) on the FP32 parameters, then the BF16 copies
-cudaError_t mlp_adam(float *p, float *m, float *v, const float *grad, float lr, int step, void *w1t, void *w2t,
-                     void *w2, cudaStream_t s);
+// Adam step `step` (1-based) on the FP32 parameters, then the BF16 copies;
+// with c12 the step's bias corrections (mlp_adam_corrections) are read from
+// device memory instead
+cudaError_t mlp_adam(float *p, float *m, float *v, const float *grad, float lr, int step, const float *c12,
+                     void *w1t, void *w2t, void *w2, cudaStream_t s);
+void mlp_adam_corrections(long long step, float *c1, float *c2);
 cudaError_t mlp_pack(const float *p, void *w1t, void *w2t, void *w2, cudaStream_t s);
 cudaError_t mlp_cell_hist(const void *data, int dtype, int nx, int ny, int nz, int cell, int mcx, int mcy, int mcz,
                           float vmin, float vmax, float *hist, cudaStream_t s);

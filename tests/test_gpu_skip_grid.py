@@ -121,9 +121,9 @@ def test_learned_grid_is_certified_and_its_own_distance_transform(ctx, oracle_mo
     tfs = [ctx.transfer_function().set_lut(t, 0, scale, api.TF_F2B) for t in luts]
     mlp = ctx.mlp(4)
     try:
-        for tf in tfs[:2]:
+        for tf in tfs[:3]:
             mlp.add_samples(v, tf)
-        mlp.train(4, batch_rows=512, lr=3e-3, wneg=4.0)
+        mlp.train(40, batch_rows=256, lr=3e-3, wneg=4.0)
         margin, _ = mlp.calibrate(0.05)
         v.set_mlp(mlp, margin, certify=True)
         learned_cells = 0
