@@ -15,6 +15,15 @@ constexpr int kMinCell = 4, kMaxCell = 32;  // the edges a volume may use: power
 #define IVR_DIST_CAP 8
 #endif
 constexpr int kDistCap = IVR_DIST_CAP;  // largest transparent radius stored per macrocell
+// f32 corner-packed copies hold each row pair as (v0, v1 - v0): the
+// sampler's x lerp fmaf(fx, v1 - v0, v0) then takes no subtraction, and
+// the difference is the same IEEE subtraction the sampler would make, so
+// every sample is bitwise unchanged.  (u8/u16 differences do not fit their
+// lanes.)  IVR_QUAD_DELTA=0 stores the voxels themselves.
+#ifndef IVR_QUAD_DELTA
+#define IVR_QUAD_DELTA 1
+#endif
+constexpr bool kQuadDelta = IVR_QUAD_DELTA != 0;
 
 // One brick as the march kernels see it.  Geometry follows the reference's
 // per-rank AABB (main.c:552-618): bmin and w/h/d from the brick's world
@@ -38,7 +47,9 @@ struct DevBrick {
     uint8_t *touched;       // census only: cells an executed sample read
     const void *quad;       // corner-packed copy or null: element (j, i, k),
                             // j < nx-1, i < ny-1, holds the voxels (j, i),
-                            // (j+1, i), (j, i+1), (j+1, i+1) of slab k
+                            // (j+1, i), (j, i+1), (j+1, i+1) of slab k (f32
+                            // with kQuadDelta: the second of each pair as
+                            // its difference from the first)
     const uint8_t *opac;    // per macrocell: 255 sqrt(mean LUT opacity over
                             // its value range) -- the tile cost estimate's
                             // input; or null

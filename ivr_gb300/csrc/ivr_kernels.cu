@@ -507,6 +507,12 @@ __global__ void quad_kernel(const T *src, int nx, int ny, int nz, V *dst)
         v.y = p[1];
         v.z = p[nx];
         v.w = p[nx + 1];
+        if constexpr (sizeof(T) == sizeof(float)) {
+            if (kQuadDelta) {  // the sampler's x-lerp differences, rounded as it rounds them
+                v.y = p[1] - p[0];
+                v.w = p[nx + 1] - p[nx];
+            }
+        }
         dst[e] = v;
     }
 }

@@ -262,6 +262,13 @@ __device__ __forceinline__ float fetch_cfg(const DevBrick &b, const CellPos &c)
             c10 = lerp23(off23(lo.y, kU16Half0), off23(lo.y, kU16Half1), fx);
             c01 = lerp23(off23(hi.x, kU16Half0), off23(hi.x, kU16Half1), fx);
             c11 = lerp23(off23(hi.y, kU16Half0), off23(hi.y, kU16Half1), fx);
+        } else if (kQuadDelta) {
+            // (v0, v1 - v0) pairs: the x lerps without their subtraction
+            const V lo = __ldg(e), hi = __ldg(e + qs);
+            c00 = fmaf(fx, (float) lo.y, (float) lo.x);
+            c10 = fmaf(fx, (float) lo.w, (float) lo.z);
+            c01 = fmaf(fx, (float) hi.y, (float) hi.x);
+            c11 = fmaf(fx, (float) hi.w, (float) hi.z);
         } else {
             const V lo = __ldg(e), hi = __ldg(e + qs);
             c00 = lerpf((float) lo.x, (float) lo.y, fx);
@@ -339,6 +346,11 @@ __device__ __forceinline__ float quad_interp(const QuadCell<DT> &q, const CellPo
         c10 = lerp23(off23(q.lo.y, kU16Half0), off23(q.lo.y, kU16Half1), c.fx);
         c01 = lerp23(off23(q.hi.x, kU16Half0), off23(q.hi.x, kU16Half1), c.fx);
         c11 = lerp23(off23(q.hi.y, kU16Half0), off23(q.hi.y, kU16Half1), c.fx);
+    } else if (kQuadDelta) {
+        c00 = fmaf(c.fx, q.lo.y, q.lo.x);
+        c10 = fmaf(c.fx, q.lo.w, q.lo.z);
+        c01 = fmaf(c.fx, q.hi.y, q.hi.x);
+        c11 = fmaf(c.fx, q.hi.w, q.hi.z);
     } else {
         c00 = lerpf(q.lo.x, q.lo.y, c.fx);
         c10 = lerpf(q.lo.z, q.lo.w, c.fx);
