@@ -497,23 +497,33 @@ int ivr_mlp_train(ivr_mlp *m, int epochs, int batch_rows, float lr, float wneg, 
         return code;
     };
     const MlpDev w = dev_of(m);
-    // the epochs' row orders in two page-locked buffers: the host shuffles
-    // the next epoch's while the device trains on the current one
+    // the epochs' row orders in two page-locked buffers (the host shuffles
+    // the next epoch's while the device trains on the current one), and the
+    // epoch's bias corrections and losses in page-locked memory too, so that
+    // no copy of an epoch waits for the host or the host for the device
+    // before the shuffle is done
     const size_t n = (size_t) m->n;
     int *order[2] = {nullptr, nullptr};
+    float *c12 = nullptr, *losses = nullptr;
     struct Pinned {
-        int **p;
+        void *p[4];
         ~Pinned()
         {
-            for (int k = 0; k < 2; k++)
-                if (p[k]) cudaFreeHost(p[k]);
+            for (void *q : p)
+                if (q) cudaFreeHost(q);
         }
-    } pinned{order};
+    } pinned{};
     SplitMix rng{m->seed ^ 0x9e3779b97f4a7c15ull};
-    std::vector<float> losses((size_t) nb), c12((size_t) (2 * nb));
     cudaError_t e = cudaDeviceSynchronize();
-    for (int k = 0; k < 2 && e == cudaSuccess; k++) e = cudaHostAlloc((void **) &order[k], sizeof(int) * n, 0);
+    if (e == cudaSuccess) e = cudaHostAlloc(&pinned.p[0], sizeof(int) * n, 0);
+    if (e == cudaSuccess) e = cudaHostAlloc(&pinned.p[1], sizeof(int) * n, 0);
+    if (e == cudaSuccess) e = cudaHostAlloc(&pinned.p[2], sizeof(float) * 2 * (size_t) nb, 0);
+    if (e == cudaSuccess) e = cudaHostAlloc(&pinned.p[3], sizeof(float) * (size_t) nb, 0);
     if (e != cudaSuccess) return done(cuda_fail(c, e, "training order buffers"));
+    order[0] = (int *) pinned.p[0];
+    order[1] = (int *) pinned.p[1];
+    c12 = (float *) pinned.p[2];
+    losses = (float *) pinned.p[3];
     for (size_t i = 0; i < n; i++) order[0][i] = (int) i;
     shuffle_rows(order[0], n, rng);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&gr.s, cudaStreamNonBlocking);
@@ -545,11 +555,11 @@ int ivr_mlp_train(ivr_mlp *m, int epochs, int batch_rows, float lr, float wneg, 
         for (long long b = 0; b < nb; b++) mlp_adam_corrections(m->step + b + 1, &c12[2 * b], &c12[2 * b + 1]);
         e = cudaMemcpyAsync(m->d_idx, order[cur], sizeof(int) * n, cudaMemcpyHostToDevice, gr.s);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d_c12, c12.data(), sizeof(float) * c12.size(), cudaMemcpyHostToDevice, gr.s);
+            e = cudaMemcpyAsync(d_c12, c12, sizeof(float) * 2 * (size_t) nb, cudaMemcpyHostToDevice, gr.s);
         if (e == cudaSuccess) e = cudaMemsetAsync(m->d_loss, 0, sizeof(float) * (size_t) nb, gr.s);
         if (e == cudaSuccess) e = cudaGraphLaunch(gr.x, gr.s);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(losses.data(), m->d_loss, sizeof(float) * (size_t) nb, cudaMemcpyDeviceToHost, gr.s);
+            e = cudaMemcpyAsync(losses, m->d_loss, sizeof(float) * (size_t) nb, cudaMemcpyDeviceToHost, gr.s);
         if (e == cudaSuccess && ep + 1 < epochs) {  // the next epoch's order, meanwhile
             memcpy(order[cur ^ 1], order[cur], sizeof(int) * n);
             shuffle_rows(order[cur ^ 1], n, rng);
@@ -559,7 +569,7 @@ int ivr_mlp_train(ivr_mlp *m, int epochs, int batch_rows, float lr, float wneg, 
         m->step += (int) nb;
         if (loss_per_epoch) {
             double sum = 0.0;
-            for (float l : losses) sum += l;
+            for (long long b = 0; b < nb; b++) sum += losses[b];
             loss_per_epoch[ep] = (float) (sum / (double) nb);
         }
     }
