@@ -174,7 +174,8 @@ int ivr_bricks_setup(ivr_volume *vol, int py, int px, int pz, int overlap);
 int ivr_volume_gradient(ivr_volume *vol, float *grad4_dev, void *stream);
 /* Corner-packed brick copies (no counterpart in the reference; on by
  * default).  Each brick gets a second copy in which element (j, i, k) holds
- * the four voxels (j, i), (j+1, i), (j, i+1), (j+1, i+1) of slab k, so a
+ * the four voxels (j, i), (j+1, i), (j, i+1), (j+1, i+1) of slab k (f32:
+ * the second of each pair as its difference from the first), so a
  * trilinear sample of the CONFIG march is two vector loads instead of eight
  * gathers.  It costs 4x the brick's bytes of HBM; a copy that does not fit
  * the budget is left out and the march reads the brick itself.  The images
