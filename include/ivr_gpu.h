@@ -350,8 +350,9 @@ int ivr_server_listen(ivr_server *server, int port, int volume, int tf, int *bou
  * one batched inference.
  *   inputs (26, zero padded to 32, BF16): the cell's min and max normalised
  *     to the volume's range, its 8-bin value histogram (fractions), and the
- *     TF's 16 knots: the largest LUT opacity over each sixteenth of the
- *     volume's value range;
+ *     TF's 16-knot encoding on 16 knots evenly spaced over the LUT's entries
+ *     (entry k (n-1)/15): the largest opacity between knots k and k + 1 for
+ *     k < 15, and the largest opacity of the LUT;
  *   network: 26 -> 64 -> 64 -> 1, ReLU, BF16 weights and activations, FP32
  *     accumulation on the tcgen05 tensor cores with accumulators in tensor
  *     memory (training, inference, and the grid of a TF in one launch);

@@ -135,7 +135,7 @@ int features(ivr_mlp *m, ivr_volume *v, const ivr_tf *tf, uint16_t *X, float *T,
     ivr_ctx *c = m->ctx;
     int rc = ensure_cell_hist(v, s);
     if (rc) return rc;
-    CK(c, mlp_tf_knots(tf->d_lut, tf->n, tf->off, tf->scale, v->vmin, v->vmax, m->d_knots, s));
+    CK(c, mlp_tf_knots(tf->d_lut, tf->n, m->d_knots, s));
     long long off = 0;
     for (size_t k = 0; k < v->bricks.size(); k++) {
         const HostBrick &b = v->bricks[k];
@@ -211,7 +211,7 @@ int ivr::learned_fields(ivr_volume *v, const ivr_tf *tf, const std::vector<uint8
     rc = ensure_cell_hist(v, s);
     if (rc) return rc;
     CK(c, cudaStreamWaitEvent(s, m->scratch_ev, 0));
-    CK(c, mlp_tf_knots(tf->d_lut, tf->n, tf->off, tf->scale, v->vmin, v->vmax, m->d_knots, s));
+    CK(c, mlp_tf_knots(tf->d_lut, tf->n, m->d_knots, s));
     const MlpDev w = dev_of(m);
     for (size_t k = 0; k < v->bricks.size(); k++) {
         const HostBrick &b = v->bricks[k];

@@ -116,18 +116,20 @@ __global__ void cell_features_kernel(const float *mc, const float *hist, int nce
     }
 }
 
-// The TF's 16-knot encoding: knot k is the largest LUT opacity over the
-// entries that values in the k-th sixteenth of [vmin, vmax] index (the same
-// index rule as the bounds).  One warp per knot.
-__global__ void tf_knots_kernel(const float4 *lut, int lut_n, int lut_off, float lut_scale, float vmin, float vmax,
-                                float *knots)
+// The TF's 16-knot encoding, on 16 knots evenly spaced over the LUT's
+// entries (entry k (n-1)/15, the knots of a piecewise-linear TF of 16
+// knots): feature k < 15 is the largest opacity between knots k and k + 1,
+// both included, and feature 15 the largest opacity of the whole LUT.  A
+// cell is transparent when every interval its index range overlaps is zero,
+// which the network can read off these and the cell's min and max.  One
+// warp per feature.
+__global__ void tf_knots_kernel(const float4 *lut, int lut_n, float *knots)
 {
     const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (k >= kMlpKnots) return;
-    const float r = vmax - vmin;
-    const float lo = vmin + r * (float) k / (float) kMlpKnots, hi = vmin + r * (float) (k + 1) / (float) kMlpKnots;
-    const int a = min(max((int) (lo * lut_scale) - 1 - lut_off, 0), lut_n - 1);
-    const int b = min(max((int) (hi * lut_scale) + 1 - lut_off, 0), lut_n - 1);
+    const int last = kMlpKnots - 1;
+    const int a = k < last ? k * (lut_n - 1) / last : 0;
+    const int b = k < last ? ((k + 1) * (lut_n - 1) + last - 1) / last : lut_n - 1;
     float m = 0.0f;
     for (int i = a + lane; i <= b; i += 32) m = fmaxf(m, lut[i].w);
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -216,10 +218,9 @@ cudaError_t mlp_cell_features(const float *mc, const float *hist, int ncell, flo
     return cudaGetLastError();
 }
 
-cudaError_t mlp_tf_knots(const float4 *lut, int lut_n, int lut_off, float lut_scale, float vmin, float vmax,
-                         float *knots, cudaStream_t s)
+cudaError_t mlp_tf_knots(const float4 *lut, int lut_n, float *knots, cudaStream_t s)
 {
-    tf_knots_kernel<<<1, 32 * kMlpKnots, 0, s>>>(lut, lut_n, lut_off, lut_scale, vmin, vmax, knots);
+    tf_knots_kernel<<<1, 32 * kMlpKnots, 0, s>>>(lut, lut_n, knots);
     return cudaGetLastError();
 }
 

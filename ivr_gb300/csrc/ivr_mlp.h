@@ -72,8 +72,7 @@ cudaError_t mlp_cell_hist(const void *data, int dtype, int nx, int ny, int nz, i
 cudaError_t mlp_cell_features(const float *mc, const float *hist, int ncell, float vmin, float vmax,
                               const float *knots_dev, const float4 *lut, int lut_n, int lut_off, float lut_scale,
                               void *X, float *targets, cudaStream_t s);
-cudaError_t mlp_tf_knots(const float4 *lut, int lut_n, int lut_off, float lut_scale, float vmin, float vmax,
-                         float *knots, cudaStream_t s);
+cudaError_t mlp_tf_knots(const float4 *lut, int lut_n, float *knots, cudaStream_t s);
 // One brick's learned grid for one TF, in one launch: each cell's features
 // (as mlp_cell_features writes them), the network (as mlp_forward runs it)
 // and the transparent flag (kDistCap / 0) of y + margin <= 0; with certify

@@ -108,15 +108,18 @@ def bound(lo, hi, lut, off, scale):
     return float(lut[a:b + 1, 3].max())
 
 
-def knots(lut, off, scale, vmin, vmax):
-    """16-knot encoding: knot k = bound over the k-th sixteenth of [vmin, vmax]."""
-    f = np.float32
-    r = f(vmax) - f(vmin)
+def knots(lut):
+    """16-knot encoding over 16 knots evenly spaced on the LUT's entries
+    (entry k (n-1)/15): feature k < 15 = the largest opacity between knots k
+    and k + 1 (entries floor(k (n-1)/15) .. ceil((k+1) (n-1)/15)), feature 15
+    = the largest opacity of the LUT."""
+    n = len(lut)
+    last = KNOTS - 1
     out = np.zeros(KNOTS, np.float32)
-    for k in range(KNOTS):
-        lo = f(vmin) + (r * f(k)) / f(KNOTS)
-        hi = f(vmin) + (r * f(k + 1)) / f(KNOTS)
-        out[k] = bound(lo, hi, lut, off, scale)
+    for k in range(last):
+        a, b = k * (n - 1) // last, ((k + 1) * (n - 1) + last - 1) // last
+        out[k] = lut[a:b + 1, 3].max()
+    out[last] = lut[:, 3].max()
     return out
 
 
@@ -133,7 +136,7 @@ def features(vol, lut, off, scale, cell=CELL):
     nz, ny, nx = v.shape
     vmin, vmax = np.float32(v.min()), np.float32(v.max())
     mcx, mcy, mcz = cell_grid(nx, ny, nz, cell)
-    kn = knots(lut, off, scale, vmin, vmax)
+    kn = knots(lut)
     inv = np.float32(1.0) / (vmax - vmin) if vmax > vmin else np.float32(0.0)
     hscale = np.float32(8.0) / (vmax - vmin) if vmax > vmin else np.float32(0.0)
     X = np.zeros((mcx * mcy * mcz, IN), np.float32)
