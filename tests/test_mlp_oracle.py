@@ -110,3 +110,22 @@ def test_features_of_a_tiny_volume():
     assert T[-1] == pytest.approx(0.5)
     # histogram rows are fractions
     np.testing.assert_allclose(X[:, 2:10].sum(axis=1), 1.0, atol=0.03)
+
+
+@pytest.mark.parametrize("seed", [1000, 1017, 1035])
+def test_knot_encoding_reads_a_16_knot_tf(seed):
+    """On a piecewise-linear TF of 16 knots (entry 17 k of 256 is knot k),
+    feature k < 15 is the larger of knots k and k + 1, and feature 15 the
+    LUT's largest opacity; every other LUT size keeps intervals that cover
+    the LUT and overlap only at their shared knot."""
+    from ivr_gb300 import synth
+    lut, ka = synth.knot_tf(seed, zero_first=True)
+    kn = M.knots(lut)
+    np.testing.assert_allclose(kn[:15], np.maximum(ka[:-1], ka[1:]), rtol=0, atol=1e-6)
+    assert kn[15] == lut[:, 3].max()
+    for n in (1, 2, 15, 16, 17, 100, 256, 4096):
+        last = M.KNOTS - 1
+        spans = [(k * (n - 1) // last, ((k + 1) * (n - 1) + last - 1) // last) for k in range(last)]
+        assert spans[0][0] == 0 and spans[-1][1] == n - 1
+        assert all(a <= b <= n - 1 for a, b in spans)
+        assert all(spans[k + 1][0] <= spans[k][1] for k in range(last - 1))
