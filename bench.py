@@ -324,7 +324,7 @@ def learned_config(args, L):
                      "none": "none (every lattice point)"}[getattr(args, "skip", "learned")],
             "step": "one frame: a new view under the next TF",
             "tile_order": "costliest first (estimated)" if getattr(args, "tiles", "raster") == "cost" else "row order",
-            "frames_in_flight": getattr(args, "inflight", 3),
+            "frames_in_flight": getattr(args, "inflight", 4),
             "l2": "inputs larger than L2 (2 GiB volume resident)", "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -748,7 +748,7 @@ def sorted_config(args, wl, name):
             "step_voxels": wl["step"], "early_termination_alpha": wl["term"],
             "skip": f"macrocell grid of {args.cell}^3-voxel cells",
             "tile_order": "costliest first (estimated)" if args.tiles == "cost" else "row order",
-            "frames_in_flight": getattr(args, "inflight", 3),
+            "frames_in_flight": getattr(args, "inflight", 4),
             "tf": "256-entry RGBA FP32 ramp", "l2": "inputs larger than L2 (volume resident, > 129 MB)",
             "parallelism": f"replicas x{args.gpus}"}
 
@@ -824,7 +824,7 @@ def run_sorted(args, quiet=False, name="sorted_brick_512"):
         p_ms += e0.elapsed_time(e1)
     plain_view.free()
     # the same three views with frames in flight (as the timed frames run):
-    # frame k renders view k mod 3, each on its own view and stream
+    # frame k renders view k mod 3 on view and stream k mod S
     pf = InFlight(ctx, args.inflight, stream, h, w)
     preps = 3
 
@@ -1276,8 +1276,9 @@ def main():
                     help="learned workloads: the skipping of the timed frames (learned grid by default)")
     ap.add_argument("--train-tfs", type=int, default=0,
                     help="learned workloads: TFs whose cells train the predictor (0: the workload's 8)")
-    ap.add_argument("--inflight", type=int, default=3,
-                    help="frames in flight: consecutive frames alternate over this many views and streams")
+    ap.add_argument("--inflight", type=int, default=4,
+                    help="frames in flight: consecutive frames alternate over this many views and streams "
+                         "(measured: 4 renders learned_1024 2-3%% faster than 3, 5 no faster)")
     ap.add_argument("--no-certify", action="store_true",
                     help="learned workloads: learned grids without the cell-by-cell check against the exact test "
                          "(the per-frame judge alone guards the frames)")
